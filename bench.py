@@ -1,0 +1,380 @@
+#!/usr/bin/env python
+"""Benchmark of the tensor-voting path on one GB300 per process.
+
+Workload (default, --config c2): a seeded synthetic 256^3 float32 volume of
+64 tubes (radius 1-3 voxels, 8-segment piecewise-linear centrelines) plus
+N(0, 0.05) noise -> 3x3 structure tensor (gradient, outer product, separable
+Gaussian sigma 1.5, 9 taps, same-size output) -> TK stick + plate voting at
+sigma 4 (w = 25, samples = 20; the plate is the exact orientation integral)
+-> per-voxel 3x3 eigendecomposition of the voted field.  One "step" is that
+whole pass over the volume; the metric is voxels per second.
+
+  value     device-resident: input already in HBM, the pipeline call
+            (tvgb_pipeline3) on device arrays, CUDA events on its stream,
+            L2 flushed (256 MiB write) between timed steps outside the events.
+  e2e       the same call with pinned HOST buffers: the host->device copy of
+            the volume and the device->host copy of the voted field,
+            eigenvalues and eigenvectors are inside the timed region.
+  roofline  the dominant kernel (k_vote3_fast): algorithmic FP32 flops per
+            launch / its average launch duration (library CUDA-event timing).
+  cpu_baseline  the reference's CPU algorithm (the C port in oracle/, the
+            reference's own sampled plate rule) on a bounded interior sample,
+            all host cores, rank 0 at N = 1 only.
+
+--impl reference runs that CPU reference alone (rank 0), one bounded sample
+per step.  Under torchrun every rank processes its own volume (weak scaling,
+no collective on the data path); the reported time is the max over ranks.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "3D tensor-vote voxels/s (σ=4): surrogate vs plain, same GB300, ≤1e-3 rel err"
+
+C2 = dict(n=256, n_tubes=64, r_range=(1.0, 3.0), noise_sd=0.05, seed=2, sigma_st=1.5, sigma=4.0, w=25, samples=20)
+
+# Algorithmic FP32 flops per in-bounds (receiver, voter) pair of the fast
+# kernel, FMA = 2, counted from the formulas in tiralib_gb300/csrc/vote3.cu:
+#   stick (power 1): q.o 2, 2ug 1, r 6, u^2 1, eta 2, term 1, term*r 3, 6 accumulations 12 = 28
+#   plate (closed form): n.o 2, 2vg 1, m 6, h 6, v^2 1, cA 2, sA 1, sB 1, identity 1,
+#                        sA*m 3, sB*h 3, 12 accumulations 24 = 51
+FLOPS_PER_PAIR = 28 + 51
+FP32_LANES_PER_SM = 128
+
+
+def pairs_count(dims, hw):
+    """Exact number of in-bounds (receiver, voter) pairs: product over axes of
+    sum_x #{o in [-hw, hw] : 0 <= x + o < s}."""
+    p = 1
+    for s in dims:
+        tot = 0
+        for x in range(s):
+            tot += min(s - 1, x + hw) - max(0, x - hw) + 1
+        p *= tot
+    return p
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason sampling during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu_index = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.gpu_index)],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        try:
+            for line in open(self.path):
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        except Exception:
+            pass
+        finally:
+            if self.path and os.path.exists(self.path):
+                os.remove(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "", 1).isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "", 1).isdigit()]
+        pw = [float(r[3]) for r in rows if r[3].replace(".", "", 1).isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "power_w_max": max(pw) if pw else None, "samples": len(rows), "reasons": reasons}
+
+
+def gpu_index_for(local_rank):
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES")
+    if vis:
+        items = [v.strip() for v in vis.split(",") if v.strip()]
+        if local_rank < len(items) and items[local_rank].isdigit():
+            return int(items[local_rank])
+    return local_rank
+
+
+def cpu_reference_sample(vol, cfg, block=16, seed=0, threads=None):
+    """The reference's CPU algorithm on one bounded sample: an interior
+    block^3 receiver block with its window halo.  Structure tensor (oracle
+    restatement of volume::gradient + gaussian_convolve3), cpu::tensorvote3's
+    stick + sampled plate (samples = cfg['samples']) for the block's
+    receivers, eigendecomposition of their voted tensors.  Returns (seconds,
+    receivers, threads)."""
+    from oracle import oracle as O
+    threads = threads or os.cpu_count() or 1
+    hw = cfg["w"] // 2
+    K = O.lib().or_ksize3(cfg["sigma_st"])
+    R = K // 2
+    n = vol.shape[0]
+    rng = np.random.default_rng(seed)
+    pad = hw + R + 1
+    z0, y0, x0 = (int(v) for v in rng.integers(pad, n - pad - block, 3))
+    t0 = time.perf_counter()
+    crop = vol[z0 - hw - R - 1:z0 + block + hw + R + 1, y0 - hw - R - 1:y0 + block + hw + R + 1,
+               x0 - hw - R - 1:x0 + block + hw + R + 1]
+    st = O.structure_tensor3(crop, cfg["sigma_st"], 0)        # valid: interior of the same-size field
+    st = st[:, 1:-1, 1:-1, 1:-1]                                # drop the gradient-only rim
+    s6 = np.moveaxis(st, 0, -1)
+    m9 = np.ascontiguousarray(s6[..., [0, 1, 2, 1, 3, 4, 2, 4, 5]].reshape(s6.shape[:3] + (3, 3)))
+    S = m9.shape[0]
+    zz, yy, xx = np.meshgrid(np.arange(hw, hw + block), np.arange(hw, hw + block), np.arange(hw, hw + block),
+                             indexing="ij")
+    rec = ((zz * S + yy) * S + xx).ravel()
+    out = O.tensorvote3_receivers(m9, rec, cfg["sigma"], 0.0, cfg["w"], 1, samples=cfg["samples"], threads=threads)
+    voted = out.reshape(-1, 9)[rec]
+    ev = O.evals3(voted)
+    O.evecs3cart(voted, ev)
+    return time.perf_counter() - t0, rec.size, threads
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    from tiralib_gb300 import workloads as W
+    cfg = C2
+    vol = W.tube_volume(cfg["n"], cfg["n_tubes"], cfg["r_range"], noise_sd=cfg["noise_sd"], seed=cfg["seed"])
+    for i in range(args.warmup):
+        cpu_reference_sample(vol, cfg, block=args.ref_block, seed=1000 + i)
+    times, nrec, th = [], 0, 1
+    for i in range(args.steps):
+        t, nrec, th = cpu_reference_sample(vol, cfg, block=args.ref_block, seed=i)
+        times.append(t)
+    total = float(np.sum(times))
+    value = args.steps * nrec / total
+    sample = (f"{args.ref_block}^3 interior receivers (+{cfg['w'] // 2}-voxel window halo) of the 256^3 volume per "
+              f"step: structure tensor, stick + {cfg['samples']}-sample plate (tira::cpu::tensorvote3's algorithm), "
+              f"3x3 eigen of the voted tensors; OpenMP over receivers")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "voxels/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": config_dict(cfg),
+        "cpu_baseline": {"value": value, "unit": "voxels/s", "cores": th, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "voxels/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def config_dict(cfg):
+    return {"workload": "C2: 256^3 tube volume -> structure tensor (sigma 1.5) -> TK stick+plate vote (sigma 4, "
+                        "w 25, samples 20) -> fused 3x3 eigendecomposition",
+            "volume": [cfg["n"]] * 3, "tubes": cfg["n_tubes"], "tube_radius": list(cfg["r_range"]),
+            "noise_sd": cfg["noise_sd"], "seed": cfg["seed"], "sigma_structure": cfg["sigma_st"],
+            "sigma_vote": cfg["sigma"], "window": cfg["w"], "samples": cfg["samples"], "power": 1,
+            "path": "plain (exact plate orientation integral, no surrogate)",
+            "l2_flush": "256 MiB write between timed steps (outside the events)"}
+
+
+def parse_profile(text):
+    out = {}
+    for line in text.strip().splitlines():
+        parts = line.split()
+        if len(parts) == 3:
+            out[parts[0]] = (int(parts[1]), float(parts[2]))
+    return out
+
+
+def profiled_traffic(kernel):
+    """DRAM bytes per launch from a committed ncu summary, if one exists."""
+    path = os.path.join(HERE, "profiles", f"{kernel}_c2.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.strip().startswith("dram_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1])
+            except ValueError:
+                return None
+    return None
+
+
+def run_ours(args, rank, world, local_rank):
+    import torch
+    import ctypes
+    import tiralib_gb300 as tv
+    from tiralib_gb300 import workloads as W
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    cfg = C2
+    vol_np = W.tube_volume(cfg["n"], cfg["n_tubes"], cfg["r_range"], noise_sd=cfg["noise_sd"], seed=cfg["seed"])
+    nvox = vol_np.size
+    dims = vol_np.shape
+    vol_h = torch.from_numpy(vol_np).pin_memory()
+    vol_d = vol_h.to(dev)
+    out_d = torch.empty((6,) + dims, device=dev)
+    ev_d = torch.empty(dims + (3,), device=dev)
+    vec_d = torch.empty(dims + (3, 3), device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    kw = dict(sigma_st=cfg["sigma_st"], sigma1=cfg["sigma"], w=cfg["w"], samples=cfg["samples"], st_mode="same",
+              out_layout="planes", evecs="cartesian")
+
+    def step():
+        tv.pipeline3(vol_d, outputs=(out_d, ev_d, vec_d), **kw)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    stream = torch.cuda.current_stream()
+    lib = tv.lib()
+    lib.tvgb_profile_enable(1)
+    buf = ctypes.create_string_buffer(1 << 14)
+    lib.tvgb_profile_read(buf, len(buf))        # clear
+    l0 = tv.launch_count()
+    times = []
+    with ClockSampler(gpu_index_for(local_rank)) as clk:
+        torch.cuda.synchronize()
+        for _ in range(args.steps):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step()
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+        torch.cuda.synchronize()
+    launches = tv.launch_count() - l0
+    lib.tvgb_profile_read(buf, len(buf))
+    lib.tvgb_profile_enable(0)
+    prof = parse_profile(buf.value.decode())
+    clocks = clk.summary()
+    t_local = float(np.sum(times)) / 1e3
+    t_max = t_local
+    if dist:
+        tt = torch.tensor([t_local], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_max = float(tt.item())
+    value = world * args.steps * nvox / t_max
+
+    # ---- end to end through the C ABI with pinned host buffers
+    out_h = torch.empty((6,) + dims).pin_memory()
+    ev_h = torch.empty(dims + (3,)).pin_memory()
+    vec_h = torch.empty(dims + (3, 3)).pin_memory()
+    vol_hn, out_hn, ev_hn, vec_hn = vol_h.numpy(), out_h.numpy(), ev_h.numpy(), vec_h.numpy()
+
+    def step_e2e():
+        tv.pipeline3(vol_hn, outputs=(out_hn, ev_hn, vec_hn), **kw)
+
+    step_e2e()
+    if dist:
+        dist.barrier()
+    e2e_times = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        step_e2e()
+        e2e_times.append(time.perf_counter() - t0)
+    t_e2e = float(np.sum(e2e_times))
+    if dist:
+        tt = torch.tensor([t_e2e], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_e2e = float(tt.item())
+    e2e_value = world * args.steps * nvox / t_e2e
+    h2d = vol_np.nbytes
+    d2h = out_h.numel() * 4 + ev_h.numel() * 4 + vec_h.numel() * 4
+
+    # ---- roofline of the dominant kernel
+    props = torch.cuda.get_device_properties(dev)
+    sms = props.multi_processor_count
+    max_mhz = clocks.get("sm_max_mhz") or 2070.0
+    peak = sms * FP32_LANES_PER_SM * 2 * max_mhz * 1e6 / 1e12
+    nl, tot_ms = prof.get("k_vote3_fast", (0, 0.0))
+    roofline = None
+    if nl:
+        avg_s = tot_ms / nl / 1e3
+        flops = pairs_count(dims, cfg["w"] // 2) * FLOPS_PER_PAIR
+        achieved = flops / avg_s / 1e12
+        roofline = {"bound": "fp32", "kernel": "k_vote3_fast", "achieved": achieved, "peak": peak,
+                    "unit": "TFLOP/s", "frac": achieved / peak,
+                    "peak_source": f"nominal FP32: {sms} SMs x {FP32_LANES_PER_SM} FMA lanes x 2 x {max_mhz:.0f} MHz "
+                                   "(max SM clock; MEASURED_PEAKS.json has no FP32 figure)",
+                    "traffic": profiled_traffic("k_vote3_fast"),
+                    "flops_per_launch": flops, "avg_launch_ms": avg_s * 1e3,
+                    "share_of_step": (tot_ms / (np.sum(times))) if np.sum(times) else None}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        t, nrec, th = cpu_reference_sample(vol_np, cfg, block=args.ref_block, seed=0)
+        cpu = {"value": nrec / t, "unit": "voxels/s", "cores": th, "kind": "port",
+               "sample": f"{args.ref_block}^3 interior receivers of the same volume (+ window halo), the reference's "
+                         f"CPU algorithm (stick + {cfg['samples']}-sample plate) in oracle/, OpenMP over receivers"}
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "voxels/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config_dict(cfg),
+            "e2e": {"value": e2e_value, "unit": "voxels/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
+            "kernels": {k: {"launches": v[0], "total_ms": v[1]} for k, v in prof.items()},
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--ref-block", type=int, default=12, help="edge of the CPU reference's receiver block")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    rank, world, local_rank = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+    run_ours(args, rank, world, local_rank)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,309 @@
+// Batched symmetric eigendecomposition kernels (3x3 and 2x2) and their C ABI.
+//
+// Replaces the reference launchers tira::cuda::evals3_symmetric /
+// evecs3spherical_symmetric / evals2_symmetric / evecs2polar_symmetric
+// (tira/functions/eigen.h:896,945,769,828) whose kernels read 36-byte AoS
+// records with strided per-thread loads and run eigenvalues and
+// eigenvectors as two passes over HBM.  Here one pass does both: a block
+// stages its tile of AoS records into shared memory with 16-byte coalesced
+// loads, each thread solves one tensor, and results leave through shared
+// memory with 16-byte coalesced stores.  HBM traffic is the algorithmic
+// minimum (read the tensor once, write each output once).
+//
+// Precise mode: a scale-invariant FP32 solve for every tensor; tensors whose
+// remaining pair is closer than 1e-4 |lambda_max| are queued in shared memory
+// and finished in FP64 by the first warps of the block with every lane busy,
+// so the FP64 pipe only sees flagged tensors.
+#include "tvgb_common.cuh"
+#include "eig_device.cuh"
+
+namespace tvgb {
+
+constexpr int EIG_BLOCK = 256;
+
+// in_layout: 9 (mat3 AoS), 6 (sym6 AoS), 60 (sym6 planes)
+template <int IN_LAYOUT>
+__device__ __forceinline__ void load_tile(const float* __restrict__ in, size_t n, size_t base, int cnt, float* s_in,
+                                          bool aligned) {
+    constexpr int NF = IN_LAYOUT == 9 ? 9 : 6;
+    if (IN_LAYOUT == 60) {
+        // planes: component c of tensor i at in[c * n + i]; store AoS into smem
+        for (int c = 0; c < 6; ++c)
+            for (int i = threadIdx.x; i < cnt; i += EIG_BLOCK) s_in[i * 6 + c] = __ldg(in + c * n + base + i);
+        return;
+    }
+    const float* src = in + base * NF;
+    const int nfl = cnt * NF;
+    if (aligned && cnt == EIG_BLOCK) {
+        const float4* s4 = reinterpret_cast<const float4*>(src);
+        float4* d4 = reinterpret_cast<float4*>(s_in);
+        for (int i = threadIdx.x; i < nfl / 4; i += EIG_BLOCK) d4[i] = __ldg(s4 + i);
+    } else {
+        for (int i = threadIdx.x; i < nfl; i += EIG_BLOCK) s_in[i] = __ldg(src + i);
+    }
+}
+
+__device__ __forceinline__ void store_tile(float* __restrict__ dst, const float* s, int nfl, bool aligned, bool full) {
+    if (aligned && full && (nfl % 4) == 0) {
+        float4* d4 = reinterpret_cast<float4*>(dst);
+        const float4* s4 = reinterpret_cast<const float4*>(s);
+        for (int i = threadIdx.x; i < nfl / 4; i += EIG_BLOCK) d4[i] = s4[i];
+    } else {
+        for (int i = threadIdx.x; i < nfl; i += EIG_BLOCK) dst[i] = s[i];
+    }
+}
+
+// EVEC_FMT: 0 none, 1 cartesian (9), 2 spherical (6).  EVALS_IN: take the
+// eigenvalues from `evals_in` (the reference's evecs3spherical contract).
+template <int IN_LAYOUT, int EVEC_FMT, bool PRECISE, bool EVALS_IN>
+__global__ void __launch_bounds__(EIG_BLOCK) k_eig3(const float* __restrict__ in, size_t n,
+                                                      const float* __restrict__ evals_in, float* __restrict__ evals,
+                                                      float* __restrict__ evecs, unsigned long long* n_refined,
+                                                      int aligned_in, int aligned_out) {
+    constexpr int NF = IN_LAYOUT == 9 ? 9 : 6;
+    constexpr int NV = EVEC_FMT == 1 ? 9 : (EVEC_FMT == 2 ? 6 : 0);
+    __shared__ __align__(16) float s_in[EIG_BLOCK * NF];
+    __shared__ __align__(16) float s_ev[EIG_BLOCK * 3];
+    __shared__ __align__(16) float s_vec[EIG_BLOCK * 9];
+    __shared__ int s_q[EIG_BLOCK];
+    __shared__ int s_qn;
+
+    for (size_t base = size_t(blockIdx.x) * EIG_BLOCK; base < n; base += size_t(gridDim.x) * EIG_BLOCK) {
+        const int cnt = int(min(size_t(EIG_BLOCK), n - base));
+        if (PRECISE && threadIdx.x == 0) s_qn = 0;
+        load_tile<IN_LAYOUT>(in, n, base, cnt, s_in, aligned_in);
+        if (EVALS_IN)
+            for (int i = threadIdx.x; i < cnt * 3; i += EIG_BLOCK) s_ev[i] = __ldg(evals_in + base * 3 + i);
+        __syncthreads();
+        const int t = threadIdx.x;
+        if (t < cnt) {
+            const float* m = s_in + t * NF;
+            float a, b, c, d, e, f;
+            if (NF == 9) { a = m[0]; b = m[1]; d = m[2]; c = m[4]; e = m[5]; f = m[8]; }
+            else { a = m[0]; b = m[1]; d = m[2]; c = m[3]; e = m[4]; f = m[5]; }
+            float ev[3], v[9];
+            if (PRECISE) {
+                float w[3];
+                bool hi;
+                if (eig3_precise_fp32(a, b, c, d, e, f, ev, v, v + 3, v + 6, w, hi)) {
+                    // queue for the FP64 phase; park w and the isolated side in s_vec
+                    s_q[atomicAdd(&s_qn, 1)] = t;
+                    v[0] = w[0]; v[1] = w[1]; v[2] = w[2]; v[3] = hi ? 1.0f : 0.0f;
+                }
+            } else {
+                if (EVALS_IN) { ev[0] = s_ev[t * 3]; ev[1] = s_ev[t * 3 + 1]; ev[2] = s_ev[t * 3 + 2]; }
+                else eval3_d(a, b, c, d, e, f, ev[0], ev[1], ev[2]);
+                if (EVEC_FMT != 0) evec3_d(a, b, c, d, e, f, ev, v, v + 3, v + 6);
+            }
+            if (!EVALS_IN) { s_ev[t * 3] = ev[0]; s_ev[t * 3 + 1] = ev[1]; s_ev[t * 3 + 2] = ev[2]; }
+            if (EVEC_FMT != 0 || PRECISE)
+                for (int k = 0; k < 9; ++k) s_vec[t * 9 + k] = v[k];
+        }
+        __syncthreads();
+        if (PRECISE) {
+            // FP64 phase over the queued tensors, every lane busy
+            const int qn = s_qn;
+            for (int j = threadIdx.x; j < qn; j += EIG_BLOCK) {
+                const int u = s_q[j];
+                const float* m = s_in + u * NF;
+                float a, b, c, d, e, f;
+                if (NF == 9) { a = m[0]; b = m[1]; d = m[2]; c = m[4]; e = m[5]; f = m[8]; }
+                else { a = m[0]; b = m[1]; d = m[2]; c = m[3]; e = m[4]; f = m[5]; }
+                const float w[3] = {s_vec[u * 9], s_vec[u * 9 + 1], s_vec[u * 9 + 2]};
+                const bool hi = s_vec[u * 9 + 3] != 0.0f;
+                float ev[3], v[9];
+                eig3_precise_fp64(a, b, c, d, e, f, w, hi, ev, v, v + 3, v + 6);
+                s_ev[u * 3] = ev[0]; s_ev[u * 3 + 1] = ev[1]; s_ev[u * 3 + 2] = ev[2];
+                for (int k = 0; k < 9; ++k) s_vec[u * 9 + k] = v[k];
+            }
+            if (threadIdx.x == 0 && n_refined && qn) atomicAdd(n_refined, (unsigned long long)qn);
+            __syncthreads();
+        }
+        if (EVEC_FMT == 2) {
+            // spherical output, packed 6 per tensor into the front of s_vec
+            float sph[6];
+            if (t < cnt) {
+                float w[9];
+                for (int k = 0; k < 9; ++k) w[k] = s_vec[t * 9 + k];
+                to_spherical_d(w, sph[0], sph[1]);
+                to_spherical_d(w + 3, sph[2], sph[3]);
+                to_spherical_d(w + 6, sph[4], sph[5]);
+            }
+            __syncthreads();
+            if (t < cnt)
+                for (int k = 0; k < 6; ++k) s_vec[t * 6 + k] = sph[k];
+            __syncthreads();
+        }
+        const bool full = cnt == EIG_BLOCK;
+        if (evals && !EVALS_IN) store_tile(evals + base * 3, s_ev, cnt * 3, aligned_out, full);
+        if (NV && evecs) store_tile(evecs + base * NV, s_vec, cnt * NV, aligned_out, full);
+        __syncthreads();
+    }
+}
+
+__global__ void k_eval2(const float4* __restrict__ m4, size_t n, float2* __restrict__ ev2) {
+    for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x) {
+        const float4 m = __ldg(m4 + i);
+        float e0, e1;
+        eval2_d(m.x, m.y, m.w, e0, e1);
+        ev2[i] = make_float2(e0, e1);
+    }
+}
+
+__global__ void k_evec2(const float4* __restrict__ m4, const float2* __restrict__ ev2, size_t n, float2* __restrict__ th2) {
+    for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x) {
+        const float4 m = __ldg(m4 + i);
+        float t0, t1;
+        evec2polar_d(m.x, m.y, m.w, __ldg(ev2 + i).x, t0, t1);
+        th2[i] = make_float2(t0, t1);
+    }
+}
+
+static int grid_for(size_t items, int per_block) {
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    size_t blocks = (items + per_block - 1) / per_block;
+    size_t cap = size_t(sms) * 8;   // persistent-style grid: a multiple of the SM count
+    if (blocks > cap) blocks = cap;
+    return int(blocks ? blocks : 1);
+}
+
+template <int IL, int EF, bool PR, bool EI>
+static int launch_eig3_t(const float* in, size_t n, const float* ev_in, float* ev, float* vec, unsigned long long* nref,
+                         cudaStream_t s) {
+    const int ai = (reinterpret_cast<uintptr_t>(in) % 16) == 0;
+    const int ao = (!ev || reinterpret_cast<uintptr_t>(ev) % 16 == 0) && (!vec || reinterpret_cast<uintptr_t>(vec) % 16 == 0);
+    {
+        KernelTimer kt_("k_eig3", s);
+        k_eig3<IL, EF, PR, EI><<<grid_for(n, EIG_BLOCK), EIG_BLOCK, 0, s>>>(in, n, ev_in, ev, vec, nref, ai, ao);
+        kt_.stop();
+    }
+    TVGB_LAUNCHED();
+    return TVGB_OK;
+}
+
+template <int IL>
+static int launch_eig3_l(const float* in, size_t n, float* ev, float* vec, int fmt, bool precise,
+                         unsigned long long* nref, cudaStream_t s) {
+    if (precise) {
+        if (fmt == 1) return launch_eig3_t<IL, 1, true, false>(in, n, nullptr, ev, vec, nref, s);
+        if (fmt == 2) return launch_eig3_t<IL, 2, true, false>(in, n, nullptr, ev, vec, nref, s);
+        return launch_eig3_t<IL, 0, true, false>(in, n, nullptr, ev, vec, nref, s);
+    }
+    if (fmt == 1) return launch_eig3_t<IL, 1, false, false>(in, n, nullptr, ev, vec, nref, s);
+    if (fmt == 2) return launch_eig3_t<IL, 2, false, false>(in, n, nullptr, ev, vec, nref, s);
+    return launch_eig3_t<IL, 0, false, false>(in, n, nullptr, ev, vec, nref, s);
+}
+
+// device-pointer entry used by the other translation units too
+int eig3_device(const float* in, int layout, size_t n, float* ev, float* vec, int fmt, bool precise,
+                unsigned long long* nref, cudaStream_t s) {
+    if (n == 0) return TVGB_OK;
+    if (layout == TVGB_LAYOUT_MAT3) return launch_eig3_l<9>(in, n, ev, vec, fmt, precise, nref, s);
+    if (layout == TVGB_LAYOUT_SYM6) return launch_eig3_l<6>(in, n, ev, vec, fmt, precise, nref, s);
+    return launch_eig3_l<60>(in, n, ev, vec, fmt, precise, nref, s);
+}
+
+}  // namespace tvgb
+
+using namespace tvgb;
+
+extern "C" {
+
+int tvgb_eig3(const float* mats, int in_layout, size_t n, float* evals3, float* evecs, int evec_format, int mode,
+              size_t* n_refined, void* stream) {
+    TVGB_CHECK_ARG(mats || n == 0, "tvgb_eig3: mats is NULL");
+    TVGB_CHECK_ARG(in_layout == TVGB_LAYOUT_MAT3 || in_layout == TVGB_LAYOUT_SYM6 || in_layout == TVGB_LAYOUT_SYM6_PLANES,
+                   "tvgb_eig3: in_layout must be 9, 6 or 60 (got %d)", in_layout);
+    TVGB_CHECK_ARG(evec_format >= 0 && evec_format <= 2, "tvgb_eig3: evec_format must be 0, 1 or 2");
+    TVGB_CHECK_ARG(mode == TVGB_EIG_PARITY || mode == TVGB_EIG_PRECISE, "tvgb_eig3: mode must be 0 or 1");
+    if (n_refined) *n_refined = 0;
+    if (n == 0) return TVGB_OK;
+    cudaStream_t s = as_stream(stream);
+    const size_t nf = in_layout == TVGB_LAYOUT_MAT3 ? 9 : 6;
+    const size_t nv = evec_format == 1 ? 9 : (evec_format == 2 ? 6 : 0);
+    DevArray din, dev_, dvec;
+    TVGB_TRY(din.in(mats, n * nf * sizeof(float), s));
+    TVGB_TRY(dev_.out(evals3, n * 3 * sizeof(float), s));
+    TVGB_TRY(dvec.out(nv ? evecs : nullptr, n * nv * sizeof(float), s));
+    Scratch cnt;
+    if (n_refined && mode == TVGB_EIG_PRECISE) {
+        TVGB_TRY(cnt.alloc(sizeof(unsigned long long), s));
+        TVGB_CUDA(cudaMemsetAsync(cnt.p, 0, sizeof(unsigned long long), s));
+    }
+    TVGB_TRY(eig3_device(din.get<float>(), in_layout, n, dev_.get<float>(), dvec.get<float>(), evec_format,
+                         mode == TVGB_EIG_PRECISE, cnt.get<unsigned long long>(), s));
+    TVGB_TRY(dev_.finish());
+    TVGB_TRY(dvec.finish());
+    bool need_sync = din.owned || dev_.owned || dvec.owned;
+    if (cnt.p) {
+        unsigned long long h = 0;
+        TVGB_CUDA(cudaMemcpyAsync(&h, cnt.p, sizeof(h), cudaMemcpyDeviceToHost, s));
+        TVGB_CUDA(cudaStreamSynchronize(s));
+        *n_refined = size_t(h);
+        need_sync = false;
+    }
+    return sync_if(need_sync, s);
+}
+
+int tvgb_evals3_symmetric(const float* mats9, size_t n, float* evals3, void* stream) {
+    TVGB_CHECK_ARG(evals3 || n == 0, "tvgb_evals3_symmetric: evals3 is NULL");
+    return tvgb_eig3(mats9, TVGB_LAYOUT_MAT3, n, evals3, nullptr, TVGB_EVEC_NONE, TVGB_EIG_PARITY, nullptr, stream);
+}
+
+int tvgb_evecs3spherical_symmetric(const float* mats9, const float* evals3, size_t n, float* evecs6, void* stream) {
+    TVGB_CHECK_ARG((mats9 && evals3 && evecs6) || n == 0, "tvgb_evecs3spherical_symmetric: NULL argument");
+    if (n == 0) return TVGB_OK;
+    cudaStream_t s = as_stream(stream);
+    DevArray din, dev_, dvec;
+    TVGB_TRY(din.in(mats9, n * 9 * sizeof(float), s));
+    TVGB_TRY(dev_.in(evals3, n * 3 * sizeof(float), s));
+    TVGB_TRY(dvec.out(evecs6, n * 6 * sizeof(float), s));
+    TVGB_TRY((launch_eig3_t<9, 2, false, true>(din.get<float>(), n, dev_.get<float>(), nullptr, dvec.get<float>(),
+                                                nullptr, s)));
+    TVGB_TRY(dvec.finish());
+    return sync_if(din.owned || dev_.owned || dvec.owned, s);
+}
+
+int tvgb_evals2_symmetric(const float* mats4, size_t n, float* evals2, void* stream) {
+    TVGB_CHECK_ARG((mats4 && evals2) || n == 0, "tvgb_evals2_symmetric: NULL argument");
+    if (n == 0) return TVGB_OK;
+    cudaStream_t s = as_stream(stream);
+    DevArray din, dout;
+    TVGB_TRY(din.in(mats4, n * 16, s));
+    TVGB_TRY(dout.out(evals2, n * 8, s));
+    TVGB_CHECK_ARG(reinterpret_cast<uintptr_t>(din.dev) % 16 == 0 && reinterpret_cast<uintptr_t>(dout.dev) % 8 == 0,
+                   "tvgb_evals2_symmetric: device arrays must be 16/8-byte aligned");
+    {
+        KernelTimer kt_("k_eval2", s);
+        k_eval2<<<grid_for(n, 256), 256, 0, s>>>(din.get<float4>(), n, dout.get<float2>());
+        kt_.stop();
+    }
+    TVGB_LAUNCHED();
+    TVGB_TRY(dout.finish());
+    return sync_if(din.owned || dout.owned, s);
+}
+
+int tvgb_evecs2polar_symmetric(const float* mats4, const float* evals2, size_t n, float* thetas2, void* stream) {
+    TVGB_CHECK_ARG((mats4 && evals2 && thetas2) || n == 0, "tvgb_evecs2polar_symmetric: NULL argument");
+    if (n == 0) return TVGB_OK;
+    cudaStream_t s = as_stream(stream);
+    DevArray din, dev_, dout;
+    TVGB_TRY(din.in(mats4, n * 16, s));
+    TVGB_TRY(dev_.in(evals2, n * 8, s));
+    TVGB_TRY(dout.out(thetas2, n * 8, s));
+    TVGB_CHECK_ARG(reinterpret_cast<uintptr_t>(din.dev) % 16 == 0 && reinterpret_cast<uintptr_t>(dev_.dev) % 8 == 0 &&
+                       reinterpret_cast<uintptr_t>(dout.dev) % 8 == 0,
+                   "tvgb_evecs2polar_symmetric: device arrays must be 16/8-byte aligned");
+    {
+        KernelTimer kt_("k_evec2", s);
+        k_evec2<<<grid_for(n, 256), 256, 0, s>>>(din.get<float4>(), dev_.get<float2>(), n, dout.get<float2>());
+        kt_.stop();
+    }
+    TVGB_LAUNCHED();
+    TVGB_TRY(dout.finish());
+    return sync_if(din.owned || dev_.owned || dout.owned, s);
+}
+
+}  // extern "C"

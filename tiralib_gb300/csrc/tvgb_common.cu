@@ -1,0 +1,150 @@
+// Host-side support of libtvgb: error state, pointer classification and
+// stream-ordered device temporaries.
+#include "tvgb_common.cuh"
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+namespace tvgb {
+
+static thread_local char g_last_error[512] = "";
+
+void set_error(const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_last_error, sizeof(g_last_error), fmt, ap);
+    va_end(ap);
+}
+
+std::atomic<unsigned long long>& launch_counter() {
+    static std::atomic<unsigned long long> c{0};
+    return c;
+}
+
+namespace {
+std::atomic<int> g_prof_on{0};
+std::mutex g_prof_mu;
+struct Pending { const char* name; cudaEvent_t a, b; };
+std::vector<Pending>& pending() { static std::vector<Pending> v; return v; }
+}  // namespace
+
+KernelTimer::KernelTimer(const char* n, cudaStream_t s) : name(n), stream(s) {
+    if (!g_prof_on.load(std::memory_order_relaxed)) return;
+    if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) { a = b = nullptr; return; }
+    cudaEventRecord(a, s);
+}
+
+void KernelTimer::stop() {
+    if (!a) return;
+    cudaEventRecord(b, stream);
+    std::lock_guard<std::mutex> g(g_prof_mu);
+    pending().push_back({name, a, b});
+    a = b = nullptr;
+}
+
+bool is_device_ptr(const void* p) {
+    if (!p) return false;
+    cudaPointerAttributes a{};
+    cudaError_t e = cudaPointerGetAttributes(&a, p);
+    if (e != cudaSuccess) {
+        cudaGetLastError();  // unregistered host memory on old runtimes
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+int DevArray::in(const void* p, size_t nbytes, cudaStream_t s) {
+    user = const_cast<void*>(p);
+    bytes = nbytes;
+    stream = s;
+    output = false;
+    if (!p || nbytes == 0) return TVGB_OK;
+    if (is_device_ptr(p)) {
+        dev = user;
+        return TVGB_OK;
+    }
+    TVGB_CUDA(cudaMallocAsync(&dev, nbytes, s));
+    owned = true;
+    TVGB_CUDA(cudaMemcpyAsync(dev, p, nbytes, cudaMemcpyHostToDevice, s));
+    return TVGB_OK;
+}
+
+int DevArray::out(void* p, size_t nbytes, cudaStream_t s, bool zero) {
+    user = p;
+    bytes = nbytes;
+    stream = s;
+    output = true;
+    if (!p || nbytes == 0) return TVGB_OK;
+    if (is_device_ptr(p)) {
+        dev = p;
+    } else {
+        TVGB_CUDA(cudaMallocAsync(&dev, nbytes, s));
+        owned = true;
+    }
+    if (zero) TVGB_CUDA(cudaMemsetAsync(dev, 0, nbytes, s));
+    return TVGB_OK;
+}
+
+int DevArray::finish() {
+    if (output && owned && dev && user)
+        TVGB_CUDA(cudaMemcpyAsync(user, dev, bytes, cudaMemcpyDeviceToHost, stream));
+    return TVGB_OK;
+}
+
+int Scratch::alloc(size_t bytes, cudaStream_t s) {
+    stream = s;
+    if (bytes == 0) return TVGB_OK;
+    TVGB_CUDA(cudaMallocAsync(&p, bytes, s));
+    return TVGB_OK;
+}
+
+}  // namespace tvgb
+
+extern "C" {
+
+const char* tvgb_last_error(void) { return tvgb::g_last_error; }
+int tvgb_version(void) { return 100; }
+unsigned long long tvgb_launch_count(void) { return tvgb::launch_counter().load(); }
+
+int tvgb_profile_enable(int on) {
+    tvgb::g_prof_on.store(on ? 1 : 0);
+    return TVGB_OK;
+}
+
+// Resolves every recorded launch (synchronising on its events) and writes
+// "name count total_ms\n" lines, one per kernel, into buf; resets the record.
+int tvgb_profile_read(char* buf, size_t buflen) {
+    std::vector<tvgb::Pending> v;
+    {
+        std::lock_guard<std::mutex> g(tvgb::g_prof_mu);
+        v.swap(tvgb::pending());
+    }
+    std::map<std::string, std::pair<long, double>> agg;
+    int status = TVGB_OK;
+    for (auto& r : v) {
+        float ms = 0.0f;
+        if (cudaEventSynchronize(r.b) != cudaSuccess || cudaEventElapsedTime(&ms, r.a, r.b) != cudaSuccess) {
+            tvgb::set_error("tvgb_profile_read: event timing failed");
+            status = TVGB_ERR_CUDA;
+        }
+        auto& e = agg[r.name];
+        e.first += 1;
+        e.second += ms;
+        cudaEventDestroy(r.a);
+        cudaEventDestroy(r.b);
+    }
+    std::string out;
+    char line[256];
+    for (auto& kv : agg) {
+        snprintf(line, sizeof line, "%s %ld %.6f\n", kv.first.c_str(), kv.second.first, kv.second.second);
+        out += line;
+    }
+    if (buf && buflen) {
+        strncpy(buf, out.c_str(), buflen - 1);
+        buf[buflen - 1] = 0;
+    }
+    return status;
+}
+
+}  // extern "C"

@@ -1,0 +1,29 @@
+// Device-pointer entry points shared between libtvgb's translation units.
+#pragma once
+#include "tvgb_common.cuh"
+
+namespace tvgb {
+
+// eigen.cu: batched 3x3 solve on device arrays
+int eig3_device(const float* in, int layout, size_t n, float* ev, float* vec, int fmt, bool precise,
+                unsigned long long* nref, cudaStream_t s);
+
+// structure.cu: fused gradient -> outer product -> separable Gaussian
+int structure_tensor3_device(const float* vol, unsigned s0, unsigned s1, unsigned s2, float sigma, int mode,
+                             float* out, int out_layout, unsigned* out_dims, cudaStream_t s);
+void structure_tensor3_dims(unsigned s0, unsigned s1, unsigned s2, float sigma, int mode, unsigned* dims);
+
+// vote3.cu: voting on device arrays (in / out in the given layouts)
+int vote3_device(const float* in, int in_layout, unsigned s0, unsigned s1, unsigned s2, const tvgb_vote3_params& p,
+                 float* out, int out_layout, float* evals3, float* evecs, int evec_format, cudaStream_t s);
+
+// window rule of the reference's Python layer (tensorvote_tk.cu:88-95)
+inline unsigned auto_window(float s1, float s2) {
+    const float sm = s2 > s1 ? s2 : s1;
+    int w = 2 * int(3.0f * sm) + 1;
+    if (w < 3) w = 3;
+    if (w % 2 == 0) w += 1;
+    return unsigned(w);
+}
+
+}  // namespace tvgb

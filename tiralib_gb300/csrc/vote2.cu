@@ -1,0 +1,316 @@
+// 2D tensor voting (TK and ATV) on sm_103a and its C ABI.
+//
+// Reference path replaced (tira/functions/tensorvote.h):
+//   tira::cuda::tensorvote :2201 -> evals2_symmetric / evecs2polar_symmetric
+//   (eigen.h:769,828, each with host round trips) -> tensorvote_tk :2126
+//   (cpu::build_neighbors2d :1223 on the host, upload, global_tensorvote_tk
+//   :2072 with threadIdx.x on the SLOW axis, so every load is strided, and a
+//   cos/sin of the voter angle per pair) or tensorvote_atv :2029.
+//
+// Here: one prep kernel solves every pixel's 2x2 once (eigen.h semantics) and
+// stores the voter record (cos th1, sin th1, stick scale, lambda0); the vote
+// kernel maps x (fast axis) to threadIdx.x so voter loads coalesce, and
+// streams the Neighbor2D table through shared memory so each entry is a
+// broadcast read.  The table itself is built on the host with the
+// reference's float arithmetic (it is O(w^2 samples) and tiny).
+#include "tvgb_internal.cuh"
+#include "eig_device.cuh"
+#include <cmath>
+#include <vector>
+
+namespace tvgb {
+
+struct Nb2 {             // tira::Neighbor2D, 48 bytes (tensorvote.h:776)
+    int du, dv;
+    float dx, dy, c1, c2, Ra, Rb, Rc, Va, Vb, Vc;
+};
+static_assert(sizeof(Nb2) == 48, "Neighbor2D must be 48 bytes");
+
+// ---------------------------------------------------------------- host table (float steps of the reference)
+static float atten_h(float dist, float sigma) {            // atv_attenuation, :35
+    if (sigma == 0.0f) return (double(dist) > 1e-12) ? 0.0f : 1.0f;
+    return std::exp(-(dist * dist) / (sigma * sigma));
+}
+static float stick_norm_2d_h(float s1, float s2, unsigned p) {   // tk_stick_norm_2d, :843
+    if (p < 1) p = 1;
+    float r = 1.0f;
+    for (unsigned k = 1; k <= p; ++k) r *= float(2 * k) / float(2 * k - 1);
+    return r / (float(3.14159265358979323846) * (s1 * s1 + s2 * s2));
+}
+static void stickvote_2d_h(float rx, float ry, float s1, float s2, unsigned power, float theta, float& Va, float& Vb,
+                           float& Vc) {                     // tk_stickvote_2d, :872
+    const float qx = std::cos(theta), qy = std::sin(theta);
+    const float dist = std::sqrt(rx * rx + ry * ry);
+    float dx = 0.0f, dy = 0.0f;
+    if (dist != 0.0f) { dx = rx / dist; dy = ry / dist; }
+    const float qTd = qx * dx + qy * dy;
+    unsigned p = power < 1 ? 1 : power;
+    const float c1 = atten_h(dist, s1), c2 = atten_h(dist, s2);
+    const float q2 = qTd * qTd, t1 = 1.0f - q2, t2 = q2;
+    float D;
+    if (p == 1) D = c1 * t1 + c2 * t2;
+    else { float e1 = t1, e2 = t2; for (unsigned i = 1; i < p; ++i) { e1 *= t1; e2 *= t2; } D = c1 * e1 + c2 * e2; }
+    const float factor = D * stick_norm_2d_h(s1, s2, power);
+    const float Ra = 1 - 2 * dx * dx, Rb = -2 * dx * dy, Rc = 1 - 2 * dy * dy;
+    const float Rqx = Ra * qx + Rb * qy, Rqy = Rb * qx + Rc * qy;
+    Va = Rqx * Rqx * factor; Vb = Rqx * Rqy * factor; Vc = Rqy * Rqy * factor;
+}
+
+static int build_table(int w, float s1, float s2, unsigned power, unsigned samples, bool stick, bool plate, Nb2* out) {
+    if (w <= 0) return 0;
+    const int hw = w / 2;
+    const float inv1 = s1 > 0 ? 1.0f / (s1 * s1) : 0.0f, inv2 = s2 > 0 ? 1.0f / (s2 * s2) : 0.0f;
+    int k = 0;
+    for (int dv = -hw; dv <= hw; dv++)
+        for (int du = -hw; du <= hw; du++) {
+            Nb2 e{};
+            e.du = du; e.dv = dv;
+            const float l2 = float(du * du + dv * dv);
+            if (stick) {
+                if (l2 != 0.0f) { const float il = 1.0f / std::sqrt(l2); e.dx = float(du) * il; e.dy = float(dv) * il; }
+                e.c1 = s1 == 0.0f ? (l2 > 1e-12f ? 0.0f : 1.0f) : std::exp(-l2 * inv1);
+                e.c2 = s2 == 0.0f ? (l2 > 1e-12f ? 0.0f : 1.0f) : std::exp(-l2 * inv2);
+                e.Ra = 1.0f - 2.0f * e.dx * e.dx; e.Rb = 0.0f - 2.0f * e.dx * e.dy; e.Rc = 1.0f - 2.0f * e.dy * e.dy;
+            }
+            if (plate && samples > 0) {      // tk_plate_numerical (2D), :1048
+                const float dth = float(3.14159265358979323846 / double(float(samples)));
+                float a = 0, b = 0, c = 0;
+                for (unsigned i = 0; i < samples; ++i) {
+                    float va, vb, vc;
+                    stickvote_2d_h(float(du), float(dv), s1, s2, power, dth * float(i), va, vb, vc);
+                    a += va; b += vb; c += vc;
+                }
+                const float wb = float(3.14159265358979323846) / float(samples);
+                e.Va = a * wb; e.Vb = b * wb; e.Vc = c * wb;
+            }
+            if (out) out[k] = e;
+            k++;
+        }
+    return k;
+}
+
+// ---------------------------------------------------------------- kernels
+// voter record: (cos th1, sin th1, stick scale, lambda0); ATV adds (l1, cos th0, sin th0)
+__global__ void k_prep2(const float4* __restrict__ in, size_t n, float4* __restrict__ V, float4* __restrict__ W) {
+    for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x) {
+        const float4 m = __ldg(in + i);
+        float l0, l1, t0, t1;
+        eval2_d(m.x, m.y, m.w, l0, l1);
+        evec2polar_d(m.x, m.y, m.w, l0, t0, t1);
+        float scale = fabsf(l1) - fabsf(l0);
+        if (l1 < 0.0f) scale = -scale;                     // tk_stick_window, :996-997
+        V[i] = make_float4(cosf(t1), sinf(t1), scale, l0);
+        if (W) W[i] = make_float4(l1, cosf(t0), sinf(t0), 0.0f);
+    }
+}
+
+constexpr int V2X = 32, V2Y = 8, NB_CHUNK = 512;
+
+template <bool STICK, bool PLATE>
+__global__ void __launch_bounds__(V2X * V2Y) k_vote2_tk(const float4* __restrict__ V, const Nb2* __restrict__ nb, int nbc,
+                                                         int s0, int s1, float eta_s, unsigned power, float4* __restrict__ out) {
+    __shared__ Nb2 snb[NB_CHUNK];
+    const int x = blockIdx.x * V2X + threadIdx.x;    // fast axis (x1)
+    const int y = blockIdx.y * V2Y + threadIdx.y;    // slow axis (x0)
+    const int tid = threadIdx.y * V2X + threadIdx.x;
+    float sa = 0, sb = 0, sc = 0, pa = 0, pb = 0, pc = 0;
+    for (int c0 = 0; c0 < nbc; c0 += NB_CHUNK) {
+        const int cn = min(NB_CHUNK, nbc - c0);
+        __syncthreads();
+        for (int i = tid; i < cn; i += V2X * V2Y) snb[i] = nb[c0 + i];
+        __syncthreads();
+        for (int k = 0; k < cn; ++k) {
+            const Nb2& e = snb[k];
+            const int r0 = y + e.dv, r1 = x + e.du;
+            if ((unsigned)r0 >= (unsigned)s0 || (unsigned)r1 >= (unsigned)s1) continue;
+            const float4 v = __ldg(V + size_t(r0) * s1 + r1);
+            if (STICK) {
+                const float qTd = v.x * e.dx + v.y * e.dy;
+                const float q2 = qTd * qTd, t1 = 1.0f - q2, t2 = q2;
+                float D;
+                if (power == 1) D = e.c1 * t1 + e.c2 * t2;
+                else { float e1 = t1, e2 = t2; for (unsigned i = 1; i < power; ++i) { e1 *= t1; e2 *= t2; } D = e.c1 * e1 + e.c2 * e2; }
+                const float Rqx = e.Ra * v.x + e.Rb * v.y, Rqy = e.Rb * v.x + e.Rc * v.y;
+                const float f = D * eta_s * v.z;
+                sa = fmaf(f * Rqx, Rqx, sa); sb = fmaf(f * Rqx, Rqy, sb); sc = fmaf(f * Rqy, Rqy, sc);
+            }
+            if (PLATE && v.w != 0.0f) {
+                pa = fmaf(v.w, e.Va, pa); pb = fmaf(v.w, e.Vb, pb); pc = fmaf(v.w, e.Vc, pc);
+            }
+        }
+    }
+    if (x < s1 && y < s0) out[size_t(y) * s1 + x] = make_float4(sa + pa, sb + pb, sb + pb, sc + pc);
+}
+
+// atv (2D, tensorvote.h:225) with atv_H (:161); out [a, b, c]
+__device__ __forceinline__ void atv2_pair(float l0, float l1, float e0x, float e0y, float e1x, float e1y, float rx,
+                                          float ry, float sigma, float& Va, float& Vb, float& Vc) {
+    const float dist = sqrtf(rx * rx + ry * ry);
+    const float c = sigma == 0.0f ? (dist > 1e-12f ? 0.0f : 1.0f) : expf(-(dist * dist) / (sigma * sigma));
+    float dx = 0.0f, dy = 0.0f;
+    if (dist != 0.0f) { dx = rx / dist; dy = ry / dist; }
+    const float Ra = 1 - 2 * dx * dx, Rb = -2 * dx * dy, Rc = 1 - 2 * dy * dy;
+    const float T1a = e1x * e1x, T1b = e1x * e1y, T1c = e1y * e1y;
+    const float T0a = e0x * e0x + T1a, T0b = e0x * e0y + T1b, T0c = e0y * e0y + T1c;
+    const float v0 = dx * (dx * T0a + dy * T0b) + dy * (dx * T0b + dy * T0c);
+    const float v1 = dx * (dx * T1a + dy * T1b) + dy * (dx * T1b + dy * T1c);
+    const float t0x = T0a * dx + T0b * dy, t0y = T0b * dx + T0c * dy;
+    const float t1x = T1a * dx + T1b * dy, t1y = T1b * dx + T1c * dy;
+    const float s1 = l1 - l0, i3 = 1.0f / 3.0f, i4 = 1.0f / 4.0f;
+    float Ha = s1 * (T1a - i3 * (T1a * v1 + 2 * (t1x * t1x)));
+    float Hb = s1 * (T1b - i3 * (T1b * v1 + 2 * (t1x * t1y)));
+    float Hc = s1 * (T1c - i3 * (T1c * v1 + 2 * (t1y * t1y)));
+    Ha += l0 * (T0a - i4 * (T0a * v0 + 2 * (t0x * t0x)));
+    Hb += l0 * (T0b - i4 * (T0b * v0 + 2 * (t0x * t0y)));
+    Hc += l0 * (T0c - i4 * (T0c * v0 + 2 * (t0y * t0y)));
+    const float Ra2 = Ra * Ra, Rb2 = Rb * Rb, Rc2 = Rc * Rc, Rab = Ra * Rb, Rbc = Rb * Rc, Rac = Ra * Rc;
+    Va = c * (Ra2 * Ha + 2 * Rab * Hb + Rb2 * Hc);
+    Vb = c * (Rb2 * Hb + Rab * Ha + Rac * Hb + Rbc * Hc);
+    Vc = c * (Rb2 * Ha + 2 * Rbc * Hb + Rc2 * Hc);
+}
+
+__global__ void __launch_bounds__(V2X * V2Y) k_vote2_atv(const float4* __restrict__ V, const float4* __restrict__ W,
+                                                          int s0, int s1, int hw, float sigma, float4* __restrict__ out) {
+    const int x = blockIdx.x * V2X + threadIdx.x, y = blockIdx.y * V2Y + threadIdx.y;
+    if (x >= s1 || y >= s0) return;
+    float oa = 0, ob = 0, oc = 0;
+    for (int v = -hw; v <= hw; ++v) {
+        const int r0 = y + v;
+        if (r0 < 0 || r0 >= s0) continue;
+        for (int u = -hw; u <= hw; ++u) {
+            const int r1 = x + u;
+            if (r1 < 0 || r1 >= s1) continue;
+            const size_t i = size_t(r0) * s1 + r1;
+            const float4 a = __ldg(V + i), b = __ldg(W + i);
+            float va, vb, vc;
+            atv2_pair(a.w, b.x, b.y, b.z, a.x, a.y, float(u), float(v), sigma, va, vb, vc);
+            oa += va; ob += vb; oc += vc;
+        }
+    }
+    out[size_t(y) * s1 + x] = make_float4(oa, ob, ob, oc);
+}
+
+static int vote2_impl(float* t_out, const float* t_in, const Nb2* host_or_dev_nb, int nbc, float s1, float s2,
+                      int power, unsigned w, unsigned S0, unsigned S1, bool stick, bool plate, unsigned samples,
+                      bool is_atv, cudaStream_t st) {
+    const size_t n = size_t(S0) * S1;
+    DevArray din, dout, dnb;
+    TVGB_TRY(din.in(t_in, n * 16, st));
+    TVGB_TRY(dout.out(t_out, n * 16, st));
+    TVGB_CHECK_ARG(reinterpret_cast<uintptr_t>(din.dev) % 16 == 0 && reinterpret_cast<uintptr_t>(dout.dev) % 16 == 0,
+                   "2D tensor fields must be 16-byte aligned");
+    if (!is_atv && !stick && !plate) {      // global_tensorvote_tk writes zeros (:2079-2085)
+        TVGB_CUDA(cudaMemsetAsync(dout.dev, 0, n * 16, st));
+        TVGB_TRY(dout.finish());
+        return sync_if(din.owned || dout.owned, st);
+    }
+    Scratch sv, sw;
+    TVGB_TRY(sv.alloc(n * 16, st));
+    if (is_atv) TVGB_TRY(sw.alloc(n * 16, st));
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    size_t blocks = (n + 255) / 256;
+    if (blocks > size_t(sms) * 16) blocks = size_t(sms) * 16;
+    {
+        KernelTimer kt_("k_prep2", st);
+        k_prep2<<<unsigned(blocks ? blocks : 1), 256, 0, st>>>(din.get<float4>(), n, sv.get<float4>(),
+                                                              is_atv ? sw.get<float4>() : nullptr);
+        kt_.stop();
+    }
+    TVGB_LAUNCHED();
+    dim3 grid(ceil_div(S1, V2X), ceil_div(S0, V2Y)), blk(V2X, V2Y);
+    if (is_atv) {
+        {
+            KernelTimer kt_("k_vote2_atv", st);
+            k_vote2_atv<<<grid, blk, 0, st>>>(sv.get<float4>(), sw.get<float4>(), int(S0), int(S1), int(w / 2), s1,
+                                              dout.get<float4>());
+            kt_.stop();
+        }
+        TVGB_LAUNCHED();
+    } else {
+        const bool use_plate = plate && samples > 0;
+        std::vector<Nb2> table;
+        const Nb2* nbp = host_or_dev_nb;
+        if (!nbp) {
+            table.resize(size_t(w) * w);
+            nbc = build_table(int(w), s1, s2, unsigned(power), samples, stick, use_plate, table.data());
+            nbp = table.data();
+        }
+        TVGB_TRY(dnb.in(nbp, size_t(nbc) * sizeof(Nb2), st));
+        const unsigned p = power < 1 ? 1u : unsigned(power);
+        const float eta_s = stick_norm_2d_h(s1, s2, p);
+        if (stick && use_plate)
+            {
+                KernelTimer kt_("k_vote2_tk", st);
+                k_vote2_tk<true, true><<<grid, blk, 0, st>>>(sv.get<float4>(), dnb.get<Nb2>(), nbc, int(S0), int(S1), eta_s, p, dout.get<float4>());
+                kt_.stop();
+            }
+        else if (stick)
+            {
+                KernelTimer kt_("k_vote2_tk", st);
+                k_vote2_tk<true, false><<<grid, blk, 0, st>>>(sv.get<float4>(), dnb.get<Nb2>(), nbc, int(S0), int(S1), eta_s, p, dout.get<float4>());
+                kt_.stop();
+            }
+        else
+            {
+                KernelTimer kt_("k_vote2_tk", st);
+                k_vote2_tk<false, true><<<grid, blk, 0, st>>>(sv.get<float4>(), dnb.get<Nb2>(), nbc, int(S0), int(S1), eta_s, p, dout.get<float4>());
+                kt_.stop();
+            }
+        TVGB_LAUNCHED();
+        if (!nbp || !host_or_dev_nb) TVGB_CUDA(cudaStreamSynchronize(st));   // the host table must outlive its copy
+    }
+    TVGB_TRY(dout.finish());
+    return sync_if(din.owned || dout.owned || dnb.owned, st);
+}
+
+}  // namespace tvgb
+
+using namespace tvgb;
+
+extern "C" {
+
+int tvgb_build_neighbors2d(int w, float sigma1, float sigma2, unsigned power, unsigned samples, int stick, int plate,
+                           void* out, int* count) {
+    TVGB_CHECK_ARG(count, "tvgb_build_neighbors2d: count is NULL");
+    TVGB_CHECK_ARG(w >= 0, "tvgb_build_neighbors2d: w must be >= 0");
+    *count = build_table(w, sigma1, sigma2, power, samples, stick != 0, plate != 0, static_cast<Nb2*>(out));
+    return TVGB_OK;
+}
+
+static int check2(const float* t_out, const float* t_in, float s1, unsigned w, const char* fn) {
+    TVGB_CHECK_ARG(t_out && t_in, "%s: NULL field pointer", fn);
+    TVGB_CHECK_ARG(s1 > 0.0f, "%s: sigma1 must be > 0", fn);
+    TVGB_CHECK_ARG(w >= 1 && (w % 2) == 1, "%s: window w must be a positive odd integer (got %u)", fn, w);
+    TVGB_CHECK_ARG(w <= 1025, "%s: window w = %u too large", fn, w);
+    return TVGB_OK;
+}
+
+int tvgb_tensorvote(float* t_out, const float* t_in, float sigma1, float sigma2, int power, unsigned w, unsigned shape0,
+                    unsigned shape1, int stick, int plate, unsigned samples, int is_atv, void* stream) {
+    TVGB_TRY(check2(t_out, t_in, sigma1, w, "tvgb_tensorvote"));
+    if (size_t(shape0) * shape1 == 0) return TVGB_OK;
+    return vote2_impl(t_out, t_in, nullptr, 0, sigma1, sigma2, power, w, shape0, shape1, stick != 0, plate != 0,
+                      samples, is_atv != 0, as_stream(stream));
+}
+
+int tvgb_tensorvote_prebuilt(float* t_out, const float* t_in, const void* host_nb, int nb_count, float sigma1,
+                             float sigma2, int power, unsigned w, unsigned shape0, unsigned shape1, int stick, int plate,
+                             unsigned samples, void* stream) {
+    TVGB_TRY(check2(t_out, t_in, sigma1, w, "tvgb_tensorvote_prebuilt"));
+    TVGB_CHECK_ARG(nb_count >= 0 && (nb_count == 0 || host_nb), "tvgb_tensorvote_prebuilt: bad neighbour table");
+    if (size_t(shape0) * shape1 == 0) return TVGB_OK;
+    if (nb_count == 0) {   // nothing to vote with: zeros, like a kernel with nb_count = 0
+        const size_t n = size_t(shape0) * shape1;
+        cudaStream_t st = as_stream(stream);
+        DevArray dout;
+        TVGB_TRY(dout.out(t_out, n * 16, st, true));
+        TVGB_TRY(dout.finish());
+        return sync_if(dout.owned, st);
+    }
+    return vote2_impl(t_out, t_in, static_cast<const Nb2*>(host_nb), nb_count, sigma1, sigma2, power, w, shape0, shape1,
+                      stick != 0, plate != 0, samples, false, as_stream(stream));
+}
+
+}  // extern "C"

@@ -1,0 +1,782 @@
+// 3D tensor voting on sm_103a: voter preparation, the stick + closed-form
+// plate (+ ball) vote with its fused eigendecomposition, the generic path
+// (any power / sample count, ATV) and the C ABI.
+//
+// Reference path replaced (tira/functions/tensorvote.h):
+//   tira::cuda::tensorvote3 :2817 -> evals3/evecs3spherical (eigen.h:896,945)
+//   -> serial host spherical->cartesian loop :2831-2858 -> _tensorvote3_tk :2741
+//   -> global_stickvote3 :2412 + global_platevote3 :2589 (two launches, each a
+//   read-modify-write of a 36-byte glm::mat3, neighbour table in global
+//   memory for w > 11, plate = `samples` stick votes per pair with a basis
+//   rebuilt per pair), or global_tensorvote3_atv :2640.
+//
+// Here:
+//   k_prep3      one pass over the input field: eigen.h's solve, the
+//                reference's spherical round trip of the eigenvectors
+//                (parity mode), and per-voter scales -> voter records.
+//   k_vote3_fast power = 1 with an exact plate (samples == 0 or >= 3):
+//                receivers tiled 32 x 8 x R per CTA, voter rows with their
+//                sigma-halo staged in shared memory, per-offset weights from
+//                a radial table (they depend on |offset|^2 only), stick and
+//                plate accumulated in registers in one pass, FP32 row
+//                partials folded into per-voxel Kahan sums, eigensolve fused
+//                into the epilogue.
+//   k_vote3_generic every other case (power > 1, samples < power + 2, ball
+//                with power > 1, ATV): one receiver per thread, exact
+//                reference arithmetic per pair.
+//
+// The plate closed form.  For voter plate normal n (unit), offset d = o/|o|,
+// c1 = exp(-|o|^2/s1^2), c2 likewise and ct = c2 - c1, the reference's plate
+// is (1/pi) * (pi/S) sum_i stick(q_i), q_i = cos(i pi/S) u + sin(i pi/S) v.
+// The summand is a trigonometric polynomial of degree 2 power + 2 in the
+// angle, so for S >= power + 2 the S-point rule equals the integral over
+// [0, pi).  With R = I - 2 d d^T, P = I - n n^T and p = P d the integral is
+//   (1/pi) R [ (pi/2) c1 P + (pi/8) ct (|p|^2 P + 2 p p^T) ] R
+// = (c1/2 + ct |p|^2 / 8) (I - m m^T) + (ct / 4) (R p)(R p)^T,   m = R n,
+// and with v = n.o, g = 1/|o|^2:  m = n - 2 v g o,  R p = -(o + v m)/|o|,
+// |p|^2 = [o != 0] - v^2 g.  The ball term (mean of unit stick votes over the
+// sphere, scaled by lambda0) is (c1/3 + ct [o != 0] / 15) I + (2 ct g / 15) o o^T.
+#include "tvgb_internal.cuh"
+#include "eig_device.cuh"
+
+namespace tvgb {
+
+constexpr int VX = 32;   // receivers per CTA along x (one warp)
+constexpr int VY = 8;    // rows of warps per CTA
+
+// ------------------------------------------------------------------ voter preparation
+
+struct PrepOut {
+    float4* A;   // (q, stick scale * sticknorm)  -- largest eigenvector
+    float4* B;   // (n, plate scale)               -- smallest eigenvector (unit)
+    float* C;    // lambda0 (ball)
+    float4* L;   // (lambda0, lambda1, lambda2, 0) -- ATV / generic
+    float4* E1;  // middle eigenvector (ATV)
+};
+
+template <int LAYOUT>
+__device__ __forceinline__ void read_tensor(const float* __restrict__ in, size_t n, size_t i, float& a, float& b,
+                                            float& c, float& d, float& e, float& f) {
+    if (LAYOUT == 9) {
+        const float* m = in + i * 9;
+        a = __ldg(m); b = __ldg(m + 1); d = __ldg(m + 2); c = __ldg(m + 4); e = __ldg(m + 5); f = __ldg(m + 8);
+    } else if (LAYOUT == 6) {
+        const float* m = in + i * 6;
+        a = __ldg(m); b = __ldg(m + 1); d = __ldg(m + 2); c = __ldg(m + 3); e = __ldg(m + 4); f = __ldg(m + 5);
+    } else {
+        a = __ldg(in + i); b = __ldg(in + n + i); d = __ldg(in + 2 * n + i);
+        c = __ldg(in + 3 * n + i); e = __ldg(in + 4 * n + i); f = __ldg(in + 5 * n + i);
+    }
+}
+
+template <int LAYOUT>
+__global__ void __launch_bounds__(256) k_prep3(const float* __restrict__ in, size_t n, PrepOut o, float sticknorm,
+                                                int parity) {
+    for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x) {
+        float a, b, c, d, e, f;
+        read_tensor<LAYOUT>(in, n, i, a, b, c, d, e, f);
+        float ev[3], v0[3], v1[3], v2[3];
+        if (parity) {
+            eval3_d(a, b, c, d, e, f, ev[0], ev[1], ev[2]);
+            evec3_d(a, b, c, d, e, f, ev, v0, v1, v2);
+            // cpu::tensorvote3 / cuda::tensorvote3 pass the eigenvectors through
+            // float (theta, phi) and back (tensorvote.h:1831-1849, 2831-2858)
+            float th, ph;
+            to_spherical_d(v0, th, ph); from_spherical_d(th, ph, v0);
+            to_spherical_d(v1, th, ph); from_spherical_d(th, ph, v1);
+            to_spherical_d(v2, th, ph); from_spherical_d(th, ph, v2);
+        } else {
+            eig3_precise_d(a, b, c, d, e, f, ev, v0, v1, v2);
+        }
+        if (o.A) {
+            const float ss = copysignf(fabsf(ev[2]) - fabsf(ev[1]), ev[2]);   // tensorvote.h:1537
+            o.A[i] = make_float4(v2[0], v2[1], v2[2], ss * sticknorm);
+        }
+        if (o.B) {
+            // plate3_numerical_device normalises the normal and skips a zero one (:2461-2465)
+            const float nn = v0[0] * v0[0] + v0[1] * v0[1] + v0[2] * v0[2];
+            float sp = copysignf(fabsf(ev[1]) - fabsf(ev[0]), ev[1]);      // :2616
+            float inv = 0.0f;
+            if (nn > 1e-12f) inv = rsqrtf(nn); else sp = 0.0f;
+            o.B[i] = make_float4(v0[0] * inv, v0[1] * inv, v0[2] * inv, sp);
+        }
+        if (o.C) o.C[i] = ev[0];
+        if (o.L) o.L[i] = make_float4(ev[0], ev[1], ev[2], 0.0f);
+        if (o.E1) o.E1[i] = make_float4(v1[0], v1[1], v1[2], 0.0f);
+    }
+}
+
+// ------------------------------------------------------------------ radial table
+// entry (8 floats) for integer |o|^2 = L2:
+//   a = (c1, ct * g, 2 g, c1/2 + ct [L2>0] / 8)
+//   b = (ct g / 8, ct g / 4, c1/3 + ct [L2>0] / 15, 2 ct g / 15)
+__device__ __forceinline__ void radial_entry(int L2, float s1, float s2, float4& a, float4& b) {
+    const float l2 = float(L2);
+    const float inv1 = s1 > 0.0f ? 1.0f / (s1 * s1) : 0.0f;
+    const float inv2 = s2 > 0.0f ? 1.0f / (s2 * s2) : 0.0f;
+    // build_neighbors3d's weights, including the sigma == 0 rule (tensorvote.h:1431-1432)
+    const float c1 = s1 == 0.0f ? (l2 > 1e-12f ? 0.0f : 1.0f) : expf(-l2 * inv1);
+    const float c2 = s2 == 0.0f ? (l2 > 1e-12f ? 0.0f : 1.0f) : expf(-l2 * inv2);
+    const float ct = c2 - c1;
+    const float g = L2 > 0 ? 1.0f / l2 : 0.0f;
+    const float dd = L2 > 0 ? 1.0f : 0.0f;
+    a = make_float4(c1, ct * g, 2.0f * g, 0.5f * c1 + 0.125f * ct * dd);
+    b = make_float4(0.125f * ct * g, 0.25f * ct * g, c1 * (1.0f / 3.0f) + ct * dd * (1.0f / 15.0f),
+                    ct * g * (2.0f / 15.0f));
+}
+
+// ------------------------------------------------------------------ fast kernel
+
+struct FastArgs {
+    const float4* A;
+    const float4* B;
+    const float* C;
+    int s0, s1, s2, hw, rows;   // rows: voter rows (offsets) staged per stage
+    float sig1, sig2;
+    float* out;
+    int out_layout;
+    float* evals;
+    float* evecs;
+    int evec_fmt;
+    int precise_eig;
+};
+
+__device__ __forceinline__ void kahan_add(float& sum, float& comp, float x) {
+    const float y = x - comp;
+    const float t = sum + y;
+    comp = (t - sum) - y;
+    sum = t;
+}
+
+// one row of voters (fixed vz, oy) against receivers j in [JLO, JHI]
+template <int R, int JLO, int JHI, bool STICK, bool PLATE, bool BALL>
+__device__ __forceinline__ void vote_row(const float4* __restrict__ rA, const float4* __restrict__ rB,
+                                         const float* __restrict__ rC, const float4* __restrict__ tbl,
+                                         const int (&zoff)[R], const float (&ozf)[R], float oyf, int L2y, int hw,
+                                         float (&tot)[R][6], float (&cmp)[R][6]) {
+    float P[R][7];
+#pragma unroll
+    for (int j = 0; j < R; ++j)
+#pragma unroll
+        for (int k = 0; k < 7; ++k) P[j][k] = 0.0f;
+    float oxf = -float(hw);
+    int off = 2 * (hw * hw + L2y);      // table float4 index of |(-hw, oy, 0)|^2
+    int step = 2 * (-2 * hw + 1);       // 2 * (2 ox + 1)
+    const int nx = 2 * hw + 1;
+#pragma unroll 1
+    for (int i = 0; i < nx; ++i) {
+        float4 A, B;
+        float lb = 0.0f;
+        if (STICK) A = rA[i];
+        if (PLATE) B = rB[i];
+        if (BALL) lb = rC[i];
+        const float ub = STICK ? fmaf(A.x, oxf, A.y * oyf) : 0.0f;
+        const float vb = PLATE ? fmaf(B.x, oxf, B.y * oyf) : 0.0f;
+#pragma unroll
+        for (int j = JLO; j <= JHI; ++j) {
+            const float4 ta = tbl[zoff[j] + off];
+            const float4 tb = (PLATE || BALL) ? tbl[zoff[j] + off + 1] : make_float4(0, 0, 0, 0);
+            const float oz = ozf[j];
+            if (STICK) {
+                // stickvote3_accumulate_kernel (tensorvote.h:1184) with power = 1
+                const float u = fmaf(A.z, oz, ub);             // q . o
+                const float k = u * ta.z;                       // 2 (q.d) / |o| ... times |o|: 2 u g
+                const float rx = fmaf(-k, oxf, A.x);
+                const float ry = fmaf(-k, oyf, A.y);
+                const float rz = fmaf(-k, oz, A.z);
+                const float eta = fmaf(ta.y, u * u, ta.x);      // c1 + ct (q.d)^2
+                const float term = A.w * eta;
+                const float t0 = term * rx, t1 = term * ry, t2 = term * rz;
+                P[j][0] = fmaf(t0, rx, P[j][0]);
+                P[j][1] = fmaf(t0, ry, P[j][1]);
+                P[j][2] = fmaf(t0, rz, P[j][2]);
+                P[j][3] = fmaf(t1, ry, P[j][3]);
+                P[j][4] = fmaf(t1, rz, P[j][4]);
+                P[j][5] = fmaf(t2, rz, P[j][5]);
+            }
+            if (PLATE) {
+                const float v = fmaf(B.z, oz, vb);             // n . o
+                const float k = v * ta.z;
+                const float mx = fmaf(-k, oxf, B.x);
+                const float my = fmaf(-k, oyf, B.y);
+                const float mz = fmaf(-k, oz, B.z);
+                const float hx = fmaf(v, mx, oxf);
+                const float hy = fmaf(v, my, oyf);
+                const float hz = fmaf(v, mz, oz);
+                const float cA = fmaf(-tb.x, v * v, ta.w);      // c1/2 + ct |p|^2 / 8
+                const float sA = B.w * cA;
+                const float sB = B.w * tb.y;                    // ct g / 4
+                P[j][6] += sA;
+                const float ax = sA * mx, ay = sA * my, az = sA * mz;
+                const float bx = sB * hx, by = sB * hy, bz = sB * hz;
+                P[j][0] = fmaf(bx, hx, fmaf(-ax, mx, P[j][0]));
+                P[j][1] = fmaf(bx, hy, fmaf(-ax, my, P[j][1]));
+                P[j][2] = fmaf(bx, hz, fmaf(-ax, mz, P[j][2]));
+                P[j][3] = fmaf(by, hy, fmaf(-ay, my, P[j][3]));
+                P[j][4] = fmaf(by, hz, fmaf(-ay, mz, P[j][4]));
+                P[j][5] = fmaf(bz, hz, fmaf(-az, mz, P[j][5]));
+            }
+            if (BALL) {
+                P[j][6] = fmaf(lb, tb.z, P[j][6]);
+                const float wb = lb * tb.w;
+                const float wx = wb * oxf, wy = wb * oyf, wz = wb * oz;
+                P[j][0] = fmaf(wx, oxf, P[j][0]);
+                P[j][1] = fmaf(wx, oyf, P[j][1]);
+                P[j][2] = fmaf(wx, oz, P[j][2]);
+                P[j][3] = fmaf(wy, oyf, P[j][3]);
+                P[j][4] = fmaf(wy, oz, P[j][4]);
+                P[j][5] = fmaf(wz, oz, P[j][5]);
+            }
+        }
+        off += step;
+        step += 4;
+        oxf += 1.0f;
+    }
+    // fold the row partials into the per-voxel Kahan sums
+#pragma unroll
+    for (int j = JLO; j <= JHI; ++j) {
+        kahan_add(tot[j][0], cmp[j][0], P[j][0] + P[j][6]);
+        kahan_add(tot[j][1], cmp[j][1], P[j][1]);
+        kahan_add(tot[j][2], cmp[j][2], P[j][2]);
+        kahan_add(tot[j][3], cmp[j][3], P[j][3] + P[j][6]);
+        kahan_add(tot[j][4], cmp[j][4], P[j][4]);
+        kahan_add(tot[j][5], cmp[j][5], P[j][5] + P[j][6]);
+    }
+}
+
+template <int R, int JLO, int JHI, bool S, bool PL, bool BA>
+__device__ __forceinline__ void row_if(int jlo, int jhi, const float4* rA, const float4* rB, const float* rC,
+                                       const float4* tbl, const int (&zoff)[R], const float (&ozf)[R], float oyf,
+                                       int L2y, int hw, float (&tot)[R][6], float (&cmp)[R][6]) {
+    if (jlo == JLO && jhi == JHI) vote_row<R, JLO, JHI, S, PL, BA>(rA, rB, rC, tbl, zoff, ozf, oyf, L2y, hw, tot, cmp);
+}
+
+// every (jlo, jhi) with 0 <= jlo <= jhi < R
+template <int R, int JLO, int JHI, bool S, bool PL, bool BA>
+__device__ __forceinline__ void row_dispatch(int jlo, int jhi, const float4* rA, const float4* rB, const float* rC,
+                                             const float4* tbl, const int (&zoff)[R], const float (&ozf)[R],
+                                             float oyf, int L2y, int hw, float (&tot)[R][6], float (&cmp)[R][6]) {
+    row_if<R, JLO, JHI, S, PL, BA>(jlo, jhi, rA, rB, rC, tbl, zoff, ozf, oyf, L2y, hw, tot, cmp);
+    if constexpr (JHI + 1 < R)
+        row_dispatch<R, JLO, JHI + 1, S, PL, BA>(jlo, jhi, rA, rB, rC, tbl, zoff, ozf, oyf, L2y, hw, tot, cmp);
+    else if constexpr (JLO + 1 < R)
+        row_dispatch<R, JLO + 1, JLO + 1, S, PL, BA>(jlo, jhi, rA, rB, rC, tbl, zoff, ozf, oyf, L2y, hw, tot, cmp);
+}
+
+__device__ __forceinline__ void write_receiver(const FastArgs& a, size_t idx, size_t n, const float* m6) {
+    float* out = a.out;
+    if (out) {
+        if (a.out_layout == TVGB_LAYOUT_MAT3) {
+            float* o = out + idx * 9;
+            o[0] = m6[0]; o[1] = m6[1]; o[2] = m6[2];
+            o[3] = m6[1]; o[4] = m6[3]; o[5] = m6[4];
+            o[6] = m6[2]; o[7] = m6[4]; o[8] = m6[5];
+        } else if (a.out_layout == TVGB_LAYOUT_SYM6) {
+            float* o = out + idx * 6;
+            for (int k = 0; k < 6; ++k) o[k] = m6[k];
+        } else {
+            for (int k = 0; k < 6; ++k) out[k * n + idx] = m6[k];
+        }
+    }
+    if (a.evals || a.evecs) {
+        float ev[3], v[9];
+        if (a.precise_eig) {
+            eig3_precise_d(m6[0], m6[1], m6[3], m6[2], m6[4], m6[5], ev, v, v + 3, v + 6);
+        } else {
+            eval3_d(m6[0], m6[1], m6[3], m6[2], m6[4], m6[5], ev[0], ev[1], ev[2]);
+            if (a.evecs) evec3_d(m6[0], m6[1], m6[3], m6[2], m6[4], m6[5], ev, v, v + 3, v + 6);
+        }
+        if (a.evals) { a.evals[idx * 3] = ev[0]; a.evals[idx * 3 + 1] = ev[1]; a.evals[idx * 3 + 2] = ev[2]; }
+        if (a.evecs) {
+            if (a.evec_fmt == TVGB_EVEC_CARTESIAN) {
+                for (int k = 0; k < 9; ++k) a.evecs[idx * 9 + k] = v[k];
+            } else {
+                float th, ph;
+                to_spherical_d(v, th, ph); a.evecs[idx * 6] = th; a.evecs[idx * 6 + 1] = ph;
+                to_spherical_d(v + 3, th, ph); a.evecs[idx * 6 + 2] = th; a.evecs[idx * 6 + 3] = ph;
+                to_spherical_d(v + 6, th, ph); a.evecs[idx * 6 + 4] = th; a.evecs[idx * 6 + 5] = ph;
+            }
+        }
+    }
+}
+
+template <int R, bool STICK, bool PLATE, bool BALL>
+__global__ void __launch_bounds__(VX * VY, 2) k_vote3_fast(FastArgs a) {
+    extern __shared__ __align__(16) float4 smem[];
+    const int hw = a.hw;
+    const int nt = 3 * hw * hw + 1;          // radial table entries
+    const int SW = VX + 2 * hw;              // staged row width
+    const int SR = VY + a.rows - 1;          // staged rows
+    float4* tbl = smem;                      // 2 * nt float4
+    float4* sA = tbl + 2 * nt;               // SR * SW
+    float4* sB = sA + (STICK ? SR * SW : 0);
+    float* sC = reinterpret_cast<float*>(sB + (PLATE ? SR * SW : 0));
+    const int tid = threadIdx.y * VX + threadIdx.x;
+    const int nthr = VX * VY;
+
+    for (int L2 = tid; L2 < nt; L2 += nthr) {
+        float4 ea, eb;
+        radial_entry(L2, a.sig1, a.sig2, ea, eb);
+        tbl[2 * L2] = ea;
+        tbl[2 * L2 + 1] = eb;
+    }
+
+    const int x0 = blockIdx.x * VX, y0 = blockIdx.y * VY, z0 = blockIdx.z * R;
+    const int s0 = a.s0, s1 = a.s1, s2 = a.s2;
+    const size_t plane = size_t(s1) * s2;
+
+    float tot[R][6], cmp[R][6];
+#pragma unroll
+    for (int j = 0; j < R; ++j)
+#pragma unroll
+        for (int k = 0; k < 6; ++k) { tot[j][k] = 0.0f; cmp[j][k] = 0.0f; }
+
+    const int vz_lo = max(0, z0 - hw), vz_hi = min(s0 - 1, z0 + R - 1 + hw);
+    for (int vz = vz_lo; vz <= vz_hi; ++vz) {
+        const int dzp = vz - z0;
+        const int jlo = max(0, dzp - hw), jhi = min(R - 1, dzp + hw);
+        int zoff[R];
+        float ozf[R];
+#pragma unroll
+        for (int j = 0; j < R; ++j) {
+            const int oz = dzp - j;
+            zoff[j] = 2 * oz * oz;
+            ozf[j] = float(oz);
+        }
+        for (int oy0 = -hw; oy0 <= hw; oy0 += a.rows) {
+            const int oy1 = min(hw, oy0 + a.rows - 1);
+            const int nrows = VY + (oy1 - oy0);
+            __syncthreads();   // previous stage fully consumed (and table built)
+            // stage voter rows y0+oy0 .. y0+VY-1+oy1, columns x0-hw .. x0+VX-1+hw
+            const int nst = nrows * SW;
+            for (int e = tid; e < nst; e += nthr) {
+                const int r = e / SW, c = e - r * SW;
+                const int gy = y0 + oy0 + r, gx = x0 - hw + c;
+                const bool in = (unsigned)gy < (unsigned)s1 && (unsigned)gx < (unsigned)s2;
+                const size_t gi = size_t(vz) * plane + size_t(gy) * s2 + gx;
+                if (STICK) sA[e] = in ? __ldg(a.A + gi) : make_float4(0, 0, 0, 0);
+                if (PLATE) sB[e] = in ? __ldg(a.B + gi) : make_float4(0, 0, 0, 0);
+                if (BALL) sC[e] = in ? __ldg(a.C + gi) : 0.0f;
+            }
+            __syncthreads();
+            for (int oy = oy0; oy <= oy1; ++oy) {
+                const int rr = threadIdx.y + (oy - oy0);
+                const int base = rr * SW + threadIdx.x;   // column of ox = -hw
+                row_dispatch<R, 0, 0, STICK, PLATE, BALL>(jlo, jhi, sA + base, sB + base, sC + base, tbl, zoff, ozf,
+                                                          float(oy), oy * oy, hw, tot, cmp);
+            }
+        }
+    }
+
+    const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
+    if (x >= s2 || y >= s1) return;
+    const size_t n = size_t(s0) * plane;
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+        const int z = z0 + j;
+        if (z >= s0) break;
+        float m6[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) m6[k] = tot[j][k];
+        write_receiver(a, size_t(z) * plane + size_t(y) * s2 + x, n, m6);
+    }
+}
+
+// ------------------------------------------------------------------ generic kernel
+// One receiver per thread, straight gather with the reference's arithmetic;
+// handles any power, a literal samples-point plate when samples < power + 2
+// (with the reference's (u, v) basis, tensorvote.h:2467-2469), the ball term
+// for any power (Gauss-Legendre x uniform-phi rule, exact for the integrand)
+// and ATV (tensorvote.h:710, :2640).
+
+struct GenArgs {
+    const float4* A;
+    const float4* B;
+    const float* C;
+    const float4* L;
+    const float4* E1;
+    int s0, s1, s2, hw;
+    float sig1, sig2;
+    unsigned power;
+    int plate_m;          // samples used for the plate (literal rule)
+    int stick, plate, ball, atv;
+    int ng, np;           // ball rule sizes
+    const float* gl;      // Gauss-Legendre nodes/weights (2 * ng floats), device
+    FastArgs o;           // output description
+};
+
+__device__ __forceinline__ void stick_pair(float* m, float dx, float dy, float dz, float c1, float c2, float qx, float qy,
+                                           float qz, unsigned power, float scale) {
+    const float qTd = qx * dx + qy * dy + qz * dz;
+    const float qTd2 = qTd * qTd;
+    float eta;
+    if (power == 1) eta = c1 * (1.0f - qTd2) + c2 * qTd2;
+    else {
+        const float t1 = 1.0f - qTd2, t2 = qTd2;
+        float e1 = t1, e2 = t2;
+        for (unsigned i = 1; i < power; ++i) { e1 *= t1; e2 *= t2; }
+        eta = c1 * e1 + c2 * e2;
+    }
+    const float rx = qx - 2.0f * qTd * dx, ry = qy - 2.0f * qTd * dy, rz = qz - 2.0f * qTd * dz;
+    const float term = scale * eta;
+    m[0] += term * rx * rx; m[1] += term * rx * ry; m[2] += term * rx * rz;
+    m[3] += term * ry * ry; m[4] += term * ry * rz; m[5] += term * rz * rz;
+}
+
+// atv (tensorvote.h:710) with atv_H (:607); m gets xx, xy, xz, yy, yz, zz
+__device__ __forceinline__ void atv_pair(float* m, float l0, float l1, float l2, float4 e1, float4 e2, float rx, float ry,
+                                         float rz, float sigma) {
+    const float dist = sqrtf(rx * rx + ry * ry + rz * rz);
+    const float c = sigma == 0.0f ? (dist > 1e-12f ? 0.0f : 1.0f) : expf(-(dist * dist) / (sigma * sigma));
+    float dx = 0.0f, dy = 0.0f, dz = 0.0f;
+    if (dist != 0.0f) { dx = rx / dist; dy = ry / dist; dz = rz / dist; }
+    const float R00 = 1.0f - 2.0f * dx * dx, R01 = -2.0f * dx * dy, R02 = -2.0f * dx * dz;
+    const float R11 = 1.0f - 2.0f * dy * dy, R12 = -2.0f * dy * dz, R22 = 1.0f - 2.0f * dz * dz;
+    float T[3][6];
+    T[0][0] = e2.x * e2.x; T[0][1] = e2.x * e2.y; T[0][2] = e2.x * e2.z; T[0][3] = e2.y * e2.y; T[0][4] = e2.y * e2.z; T[0][5] = e2.z * e2.z;
+    T[1][0] = e1.x * e1.x + T[0][0]; T[1][1] = e1.x * e1.y + T[0][1]; T[1][2] = e1.x * e1.z + T[0][2];
+    T[1][3] = e1.y * e1.y + T[0][3]; T[1][4] = e1.y * e1.z + T[0][4]; T[1][5] = e1.z * e1.z + T[0][5];
+    T[2][0] = 1; T[2][1] = 0; T[2][2] = 0; T[2][3] = 1; T[2][4] = 0; T[2][5] = 1;
+    const float s[3] = {l2 - l1, l1 - l0, l0};
+    const float inv[3] = {1.0f / 3.0f, 1.0f / 4.0f, 1.0f / 5.0f};
+    float H[6] = {0, 0, 0, 0, 0, 0};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float* t = T[k];   // xx xy xz yy yz zz
+        const float tvx = t[0] * dx + t[1] * dy + t[2] * dz;
+        const float tvy = t[1] * dx + t[3] * dy + t[4] * dz;
+        const float tvz = t[2] * dx + t[4] * dy + t[5] * dz;
+        const float vTv = dx * tvx + dy * tvy + dz * tvz;
+        const float tv[6] = {tvx * tvx, tvx * tvy, tvx * tvz, tvy * tvy, tvy * tvz, tvz * tvz};
+#pragma unroll
+        for (int i = 0; i < 6; ++i) H[i] += s[k] * (t[i] - inv[k] * (t[i] * vTv + 2.0f * tv[i]));
+    }
+    // V = c R H R
+    const float Hm[3][3] = {{H[0], H[1], H[2]}, {H[1], H[3], H[4]}, {H[2], H[4], H[5]}};
+    const float Rm[3][3] = {{R00, R01, R02}, {R01, R11, R12}, {R02, R12, R22}};
+    float M[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) M[i][j] = Rm[i][0] * Hm[0][j] + Rm[i][1] * Hm[1][j] + Rm[i][2] * Hm[2][j];
+    const int ii[6] = {0, 0, 0, 1, 1, 2}, jj[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+    for (int q = 0; q < 6; ++q)
+        m[q] += c * (M[ii[q]][0] * Rm[0][jj[q]] + M[ii[q]][1] * Rm[1][jj[q]] + M[ii[q]][2] * Rm[2][jj[q]]);
+}
+
+__global__ void __launch_bounds__(128) k_vote3_generic(GenArgs g) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y;
+    const int z = blockIdx.z;
+    if (x >= g.s2) return;
+    const int hw = g.hw;
+    const size_t plane = size_t(g.s1) * g.s2;
+    const float inv1 = g.sig1 > 0.0f ? 1.0f / (g.sig1 * g.sig1) : 0.0f;
+    const float inv2 = g.sig2 > 0.0f ? 1.0f / (g.sig2 * g.sig2) : 0.0f;
+    float acc[6] = {0, 0, 0, 0, 0, 0};
+    for (int dw = -hw; dw <= hw; ++dw) {
+        const int r0 = z + dw;
+        if ((unsigned)r0 >= (unsigned)g.s0) continue;
+        float row[6] = {0, 0, 0, 0, 0, 0};
+        for (int dv = -hw; dv <= hw; ++dv) {
+            const int r1 = y + dv;
+            if ((unsigned)r1 >= (unsigned)g.s1) continue;
+            for (int du = -hw; du <= hw; ++du) {
+                const int r2 = x + du;
+                if ((unsigned)r2 >= (unsigned)g.s2) continue;
+                const size_t b = size_t(r0) * plane + size_t(r1) * g.s2 + r2;
+                if (g.atv) {
+                    const float4 L = g.L[b];
+                    atv_pair(row, L.x, L.y, L.z, g.E1[b], g.A[b], float(du), float(dv), float(dw), g.sig1);
+                    continue;
+                }
+                const float l2 = float(du * du + dv * dv + dw * dw);
+                float dx = 0.0f, dy = 0.0f, dz = 0.0f;
+                if (l2 != 0.0f) { const float L = sqrtf(l2); dx = float(du) / L; dy = float(dv) / L; dz = float(dw) / L; }
+                const float c1 = g.sig1 == 0.0f ? (l2 > 1e-12f ? 0.0f : 1.0f) : expf(-l2 * inv1);
+                const float c2 = g.sig2 == 0.0f ? (l2 > 1e-12f ? 0.0f : 1.0f) : expf(-l2 * inv2);
+                if (g.stick) {
+                    const float4 A = g.A[b];
+                    stick_pair(row, dx, dy, dz, c1, c2, A.x, A.y, A.z, g.power, A.w);
+                }
+                if (g.plate) {
+                    const float4 B = g.B[b];
+                    if (B.w != 0.0f) {
+                        const float ax = fabsf(B.z) < 0.999f ? 0.0f : 1.0f, az = fabsf(B.z) < 0.999f ? 1.0f : 0.0f;
+                        // u = normalize(cross(a, n)), v = cross(n, u)   (tensorvote.h:2467-2469)
+                        float ux = 0.0f * B.z - az * B.y, uy = az * B.x - ax * B.z, uz = ax * B.y - 0.0f * B.x;
+                        const float ul = ux * ux + uy * uy + uz * uz;
+                        if (ul > 0.0f) { const float il = rsqrtf(ul); ux *= il; uy *= il; uz *= il; }
+                        const float vx = B.y * uz - B.z * uy, vy = B.z * ux - B.x * uz, vz = B.x * uy - B.y * ux;
+                        const float db = 3.14159265358979323846f / float(g.plate_m);
+                        float p[6] = {0, 0, 0, 0, 0, 0};
+                        for (int i = 0; i < g.plate_m; ++i) {
+                            float sb, cb;
+                            sincosf(db * float(i), &sb, &cb);
+                            stick_pair(p, dx, dy, dz, c1, c2, cb * ux + sb * vx, cb * uy + sb * vy, cb * uz + sb * vz,
+                                       g.power, 1.0f);
+                        }
+                        const float sw = B.w * db * (1.0f / 3.14159265358979323846f);
+                        for (int k = 0; k < 6; ++k) row[k] += sw * p[k];
+                    }
+                }
+                if (g.ball) {
+                    const float lb = g.C[b];
+                    if (lb != 0.0f) {
+                        float p[6] = {0, 0, 0, 0, 0, 0};
+                        for (int i = 0; i < g.ng; ++i) {
+                            const float ct = g.gl[i], wgt = g.gl[g.ng + i], st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct));
+                            for (int k = 0; k < g.np; ++k) {
+                                float sp, cp;
+                                sincosf(6.28318530717958647692f * float(k) / float(g.np), &sp, &cp);
+                                stick_pair(p, dx, dy, dz, c1, c2, st * cp, st * sp, ct, g.power,
+                                           wgt * (6.28318530717958647692f / float(g.np)));
+                            }
+                        }
+                        const float sw = lb * (1.0f / (4.0f * 3.14159265358979323846f));
+                        for (int k = 0; k < 6; ++k) row[k] += sw * p[k];
+                    }
+                }
+            }
+        }
+        for (int k = 0; k < 6; ++k) acc[k] += row[k];
+    }
+    write_receiver(g.o, size_t(z) * plane + size_t(y) * g.s2 + x, size_t(g.s0) * plane, acc);
+}
+
+// ------------------------------------------------------------------ host side
+
+static double factorial_d(unsigned n) {
+    double f = 1;
+    for (unsigned i = 1; i <= n; i++) f *= i;
+    return f;
+}
+
+// sticknorm3 (tensorvote.h:1163), evaluated with the reference's float steps
+static float sticknorm3_f(float s1, float s2, unsigned p) {
+    const double pi = 3.14159265358979323846;
+    const float pi_term = float(pi * std::sqrt(pi) / 2.0);
+    const float sig1_3 = s1 * s1 * s1, sig2_3 = s2 * s2 * s2;
+    const float num1 = float(std::pow(2.0, double(2 * p + 1)) * factorial_d(p) * factorial_d(p));
+    const float num2 = 2.0f;
+    const float den1 = float(factorial_d(2 * p + 1));
+    const float den2 = float(2 * p + 1);
+    return pi_term * ((sig1_3 * num1 / den1) + (sig2_3 * num2 / den2));
+}
+
+static void gauss_legendre(int n, double* x, double* w) {
+    const double pi = 3.14159265358979323846;
+    for (int i = 0; i < n; ++i) {
+        double z = std::cos(pi * (i + 0.75) / (n + 0.5)), pp = 0;
+        for (int it = 0; it < 100; ++it) {
+            double p1 = 1, p2 = 0;
+            for (int j = 0; j < n; ++j) { const double p3 = p2; p2 = p1; p1 = ((2 * j + 1) * z * p2 - j * p3) / (j + 1); }
+            pp = n * (z * p1 - p2) / (z * z - 1);
+            const double z1 = z;
+            z = z1 - p1 / pp;
+            if (std::fabs(z - z1) < 1e-15) break;
+        }
+        x[i] = z;
+        w[i] = 2 / ((1 - z * z) * pp * pp);
+    }
+}
+
+template <int R, bool S, bool P, bool B>
+static int launch_fast_t(const FastArgs& a, cudaStream_t st) {
+    const int hw = a.hw;
+    const int nt = 3 * hw * hw + 1;
+    const int SW = VX + 2 * hw;
+    const int SR = VY + a.rows - 1;
+    const size_t smem = size_t(2 * nt) * 16 + (S ? size_t(SR) * SW * 16 : 0) + (P ? size_t(SR) * SW * 16 : 0) +
+                        (B ? size_t(SR) * SW * 4 : 0);
+    TVGB_CUDA(cudaFuncSetAttribute(k_vote3_fast<R, S, P, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    dim3 grid(ceil_div(a.s2, VX), ceil_div(a.s1, VY), ceil_div(a.s0, R));
+    {
+        KernelTimer kt_("k_vote3_fast", st);
+        k_vote3_fast<R, S, P, B><<<grid, dim3(VX, VY), smem, st>>>(a);
+        kt_.stop();
+    }
+    TVGB_LAUNCHED();
+    return TVGB_OK;
+}
+
+constexpr int FAST_R = 4;
+
+static size_t fast_smem(int hw, int rows, bool S, bool P, bool B) {
+    const int nt = 3 * hw * hw + 1, SW = VX + 2 * hw, SR = VY + rows - 1;
+    return size_t(2 * nt) * 16 + (S ? size_t(SR) * SW * 16 : 0) + (P ? size_t(SR) * SW * 16 : 0) +
+           (B ? size_t(SR) * SW * 4 : 0);
+}
+
+static int launch_fast(FastArgs a, bool S, bool P, bool B, cudaStream_t st) {
+    // rows per stage: the largest count that keeps two CTAs per SM (<= ~100 KB each)
+    const int w = 2 * a.hw + 1;
+    int rows = w;
+    while (rows > 1 && fast_smem(a.hw, rows, S, P, B) > 100 * 1024) rows = (rows + 1) / 2;
+    if (fast_smem(a.hw, rows, S, P, B) > 200 * 1024) {
+        set_error("vote window too large for the shared-memory tile (w = %d)", w);
+        return TVGB_ERR_UNSUPPORTED;
+    }
+    a.rows = rows;
+    const int code = (S ? 4 : 0) | (P ? 2 : 0) | (B ? 1 : 0);
+    switch (code) {
+        case 4: return launch_fast_t<FAST_R, true, false, false>(a, st);
+        case 2: return launch_fast_t<FAST_R, false, true, false>(a, st);
+        case 6: return launch_fast_t<FAST_R, true, true, false>(a, st);
+        case 7: return launch_fast_t<FAST_R, true, true, true>(a, st);
+        case 5: return launch_fast_t<FAST_R, true, false, true>(a, st);
+        case 3: return launch_fast_t<FAST_R, false, true, true>(a, st);
+        case 1: return launch_fast_t<FAST_R, false, false, true>(a, st);
+        default: return TVGB_OK;
+    }
+}
+
+template <int LAYOUT>
+static int launch_prep_t(const float* in, size_t n, PrepOut o, float sn, int parity, cudaStream_t st) {
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    size_t blocks = (n + 255) / 256;
+    if (blocks > size_t(sms) * 16) blocks = size_t(sms) * 16;
+    {
+        KernelTimer kt_("k_prep3", st);
+        k_prep3<LAYOUT><<<unsigned(blocks ? blocks : 1), 256, 0, st>>>(in, n, o, sn, parity);
+        kt_.stop();
+    }
+    TVGB_LAUNCHED();
+    return TVGB_OK;
+}
+
+static int launch_prep(const float* in, int layout, size_t n, PrepOut o, float sn, int parity, cudaStream_t st) {
+    if (layout == TVGB_LAYOUT_MAT3) return launch_prep_t<9>(in, n, o, sn, parity, st);
+    if (layout == TVGB_LAYOUT_SYM6) return launch_prep_t<6>(in, n, o, sn, parity, st);
+    return launch_prep_t<60>(in, n, o, sn, parity, st);
+}
+
+int vote3_device(const float* in, int in_layout, unsigned s0, unsigned s1, unsigned s2, const tvgb_vote3_params& p,
+                 float* out, int out_layout, float* evals3, float* evecs, int evec_format, cudaStream_t st) {
+    const size_t n = size_t(s0) * s1 * s2;
+    if (n == 0) return TVGB_OK;
+    const unsigned w = p.w ? p.w : auto_window(p.sigma1, p.sigma2);
+    const int hw = int(w / 2);
+    const unsigned power = p.power < 1 ? 1 : p.power;
+    const bool atv = p.is_atv != 0;
+    const bool S = !atv && p.stick, P = !atv && p.plate, B = !atv && p.ball;
+    // exact plate whenever the rule has at least power + 2 points (or is the closed form)
+    const bool plate_exact = p.samples == 0 || p.samples >= power + 2;
+    const bool fast = !atv && power == 1 && (!P || plate_exact);
+
+    Scratch sA, sB, sC, sL, sE1, sGL;
+    PrepOut po{};
+    if (S || atv) { TVGB_TRY(sA.alloc(n * 16, st)); po.A = sA.get<float4>(); }
+    if (P) { TVGB_TRY(sB.alloc(n * 16, st)); po.B = sB.get<float4>(); }
+    if (B) { TVGB_TRY(sC.alloc(n * 4, st)); po.C = sC.get<float>(); }
+    if (atv) {
+        TVGB_TRY(sL.alloc(n * 16, st)); po.L = sL.get<float4>();
+        TVGB_TRY(sE1.alloc(n * 16, st)); po.E1 = sE1.get<float4>();
+    }
+    const float sn = S ? 1.0f / sticknorm3_f(p.sigma1, p.sigma2, power) : 1.0f;
+    TVGB_TRY(launch_prep(in, in_layout, n, po, sn, p.parity, st));
+
+    FastArgs fa{};
+    fa.A = po.A; fa.B = po.B; fa.C = po.C;
+    fa.s0 = int(s0); fa.s1 = int(s1); fa.s2 = int(s2); fa.hw = hw;
+    fa.sig1 = p.sigma1; fa.sig2 = p.sigma2;
+    fa.out = out; fa.out_layout = out_layout; fa.evals = evals3; fa.evecs = evecs; fa.evec_fmt = evec_format;
+    fa.precise_eig = p.parity ? 0 : 1;
+    if (!S && !P && !B && !atv) {
+        // nothing votes: the reference leaves the zeroed output
+        if (out) TVGB_CUDA(cudaMemsetAsync(out, 0, n * (out_layout == TVGB_LAYOUT_MAT3 ? 36 : 24), st));
+        if (!evals3 && !evecs) return TVGB_OK;
+    }
+    if (fast) return launch_fast(fa, S, P, B, st);
+
+    GenArgs g{};
+    g.A = po.A; g.B = po.B; g.C = po.C; g.L = po.L; g.E1 = po.E1;
+    g.s0 = int(s0); g.s1 = int(s1); g.s2 = int(s2); g.hw = hw;
+    g.sig1 = p.sigma1; g.sig2 = p.sigma2; g.power = power;
+    g.plate_m = int(plate_exact ? power + 2 : p.samples);
+    g.stick = S; g.plate = P; g.ball = B; g.atv = atv;
+    g.o = fa;
+    if (B) {
+        g.ng = int(power) + 3;
+        g.np = 2 * int(power) + 5;
+        double gx[64], gw[64];
+        gauss_legendre(g.ng, gx, gw);
+        float h[128];
+        for (int i = 0; i < g.ng; ++i) { h[i] = float(gx[i]); h[g.ng + i] = float(gw[i]); }
+        TVGB_TRY(sGL.alloc(sizeof(float) * 2 * g.ng, st));
+        TVGB_CUDA(cudaMemcpyAsync(sGL.p, h, sizeof(float) * 2 * g.ng, cudaMemcpyHostToDevice, st));
+        TVGB_CUDA(cudaStreamSynchronize(st));   // h is a stack buffer
+        g.gl = sGL.get<float>();
+    }
+    dim3 grid(ceil_div(s2, 128), s1, s0);
+    {
+        KernelTimer kt_("k_vote3_generic", st);
+        k_vote3_generic<<<grid, 128, 0, st>>>(g);
+        kt_.stop();
+    }
+    TVGB_LAUNCHED();
+    return TVGB_OK;
+}
+
+}  // namespace tvgb
+
+using namespace tvgb;
+
+extern "C" {
+
+double tvgb_sticknorm3(float sigma1, float sigma2, unsigned power) { return sticknorm3_f(sigma1, sigma2, power); }
+
+static int check_params(const tvgb_vote3_params* p, const char* fn) {
+    TVGB_CHECK_ARG(p, "%s: params is NULL", fn);
+    TVGB_CHECK_ARG(p->sigma1 >= 0.0f && p->sigma2 >= 0.0f, "%s: sigmas must be >= 0", fn);
+    TVGB_CHECK_ARG(p->is_atv || p->sigma1 > 0.0f || p->sigma2 > 0.0f, "%s: sigma1 and sigma2 are both 0", fn);
+    TVGB_CHECK_ARG(p->w == 0 || (p->w % 2) == 1, "%s: window w must be odd (got %u)", fn, p->w);
+    TVGB_CHECK_ARG(p->w <= 129, "%s: window w = %u exceeds the supported maximum 129", fn, p->w);
+    TVGB_CHECK_ARG(p->power <= 32, "%s: power = %u exceeds the supported maximum 32", fn, p->power);
+    return TVGB_OK;
+}
+
+int tvgb_vote3(const float* in, int in_layout, unsigned s0, unsigned s1, unsigned s2, const tvgb_vote3_params* p,
+               float* out, int out_layout, float* evals3, float* evecs, int evec_format, void* stream) {
+    TVGB_TRY(check_params(p, "tvgb_vote3"));
+    TVGB_CHECK_ARG(in_layout == TVGB_LAYOUT_MAT3 || in_layout == TVGB_LAYOUT_SYM6 || in_layout == TVGB_LAYOUT_SYM6_PLANES,
+                   "tvgb_vote3: in_layout must be 9, 6 or 60");
+    TVGB_CHECK_ARG(out_layout == TVGB_LAYOUT_MAT3 || out_layout == TVGB_LAYOUT_SYM6 || out_layout == TVGB_LAYOUT_SYM6_PLANES,
+                   "tvgb_vote3: out_layout must be 9, 6 or 60");
+    TVGB_CHECK_ARG(evec_format >= 0 && evec_format <= 2, "tvgb_vote3: evec_format must be 0, 1 or 2");
+    const size_t n = size_t(s0) * s1 * s2;
+    if (n == 0) return TVGB_OK;
+    TVGB_CHECK_ARG(in, "tvgb_vote3: input is NULL");
+    cudaStream_t st = as_stream(stream);
+    const size_t nin = in_layout == TVGB_LAYOUT_MAT3 ? 9 : 6, nout = out_layout == TVGB_LAYOUT_MAT3 ? 9 : 6;
+    const size_t nv = evec_format == 1 ? 9 : (evec_format == 2 ? 6 : 0);
+    DevArray din, dout, dev_, dvec;
+    TVGB_TRY(din.in(in, n * nin * 4, st));
+    TVGB_TRY(dout.out(out, n * nout * 4, st));
+    TVGB_TRY(dev_.out(evals3, n * 12, st));
+    TVGB_TRY(dvec.out(nv ? evecs : nullptr, n * nv * 4, st));
+    TVGB_TRY(vote3_device(din.get<float>(), in_layout, s0, s1, s2, *p, dout.get<float>(), out_layout,
+                          dev_.get<float>(), dvec.get<float>(), nv ? evec_format : 0, st));
+    TVGB_TRY(dout.finish());
+    TVGB_TRY(dev_.finish());
+    TVGB_TRY(dvec.finish());
+    return sync_if(din.owned || dout.owned || dev_.owned || dvec.owned, st);
+}
+
+int tvgb_tensorvote3(const float* input_field, float* output_field, unsigned s0, unsigned s1, unsigned s2, float sigma,
+                     float sigma2, unsigned w, unsigned power, int device, int stick, int plate, unsigned samples,
+                     int is_atv, void* stream) {
+    TVGB_CHECK_ARG(input_field && output_field, "tvgb_tensorvote3: NULL field pointer");
+    TVGB_CHECK_ARG(w >= 1 && (w % 2) == 1, "tvgb_tensorvote3: window w must be odd and >= 1 (got %u)", w);
+    if (device >= 0) TVGB_CUDA(cudaSetDevice(device));
+    tvgb_vote3_params p{};
+    p.sigma1 = sigma; p.sigma2 = sigma2; p.w = w; p.power = power; p.samples = samples;
+    p.stick = stick; p.plate = plate; p.ball = 0; p.is_atv = is_atv; p.parity = 1;
+    return tvgb_vote3(input_field, TVGB_LAYOUT_MAT3, s0, s1, s2, &p, output_field, TVGB_LAYOUT_MAT3, nullptr, nullptr,
+                      0, stream);
+}
+
+}  // extern "C"
