@@ -168,7 +168,7 @@ def run_reference(args, rank):
     if rank != 0:
         return
     from tiralib_gb300 import workloads as W
-    cfg = C2
+    cfg = dict(C2, n=args.size)
     vol = W.tube_volume(cfg["n"], cfg["n_tubes"], cfg["r_range"], noise_sd=cfg["noise_sd"], seed=cfg["seed"])
     for i in range(args.warmup):
         cpu_reference_sample(vol, cfg, block=args.ref_block, seed=1000 + i)
@@ -193,7 +193,8 @@ def run_reference(args, rank):
 
 
 def config_dict(cfg):
-    return {"workload": "C2: 256^3 tube volume -> structure tensor (sigma 1.5) -> TK stick+plate vote (sigma 4, "
+    n = cfg["n"]
+    return {"workload": f"C2: {n}^3 tube volume -> structure tensor (sigma 1.5) -> TK stick+plate vote (sigma 4, "
                         "w 25, samples 20) -> fused 3x3 eigendecomposition",
             "volume": [cfg["n"]] * 3, "tubes": cfg["n_tubes"], "tube_radius": list(cfg["r_range"]),
             "noise_sd": cfg["noise_sd"], "seed": cfg["seed"], "sigma_structure": cfg["sigma_st"],
@@ -237,7 +238,7 @@ def run_ours(args, rank, world, local_rank):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=dev)
-    cfg = C2
+    cfg = dict(C2, n=args.size)
     vol_np = W.tube_volume(cfg["n"], cfg["n_tubes"], cfg["r_range"], noise_sd=cfg["noise_sd"], seed=cfg["seed"])
     nvox = vol_np.size
     dims = vol_np.shape
@@ -366,6 +367,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--ref-block", type=int, default=12, help="edge of the CPU reference's receiver block")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--size", type=int, default=256, help="volume edge (256 = the benchmark workload; smaller "
+                                                          "sizes are for profiler captures)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

@@ -7,7 +7,7 @@ import ctypes
 import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "_build", "libtvgb.so")
+LIB_PATH = os.environ.get("TVGB_LIB") or os.path.join(HERE, "_build", "libtvgb.so")
 
 TVGB_OK = 0
 ERRORS = {1: "invalid argument", 2: "CUDA error", 3: "out of device memory", 4: "unsupported"}

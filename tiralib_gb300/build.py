@@ -30,14 +30,15 @@ def _flags():
                    "-Xcompiler", "-fPIC", "-Xcompiler", "-O2", "-I", os.path.join(HERE, "..", "include")]
 
 
-def build(verbose=False, extra=()):
-    os.makedirs(OUT_DIR, exist_ok=True)
+def build(verbose=False, extra=(), out_dir=None):
+    out_dir = out_dir or OUT_DIR
+    os.makedirs(out_dir, exist_ok=True)
     nvcc = nvcc_path()
     srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
     objs = []
 
     def compile_one(src):
-        obj = os.path.join(OUT_DIR, os.path.basename(src)[:-3] + ".o")
+        obj = os.path.join(out_dir, os.path.basename(src)[:-3] + ".o")
         cmd = [nvcc, "-c", src, "-o", obj] + _flags() + list(extra)
         if verbose:
             print(" ".join(cmd), flush=True)
@@ -50,15 +51,19 @@ def build(verbose=False, extra=()):
 
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(srcs), os.cpu_count() or 4))) as ex:
         objs = list(ex.map(compile_one, srcs))
-    tmp = LIB + ".tmp"
+    lib = os.path.join(out_dir, "libtvgb.so")
+    tmp = lib + ".tmp"
     cmd = [nvcc, "-shared", "-o", tmp] + objs + ARCH + ["-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":
-    extra = sys.argv[1:]
-    print(build(verbose=True, extra=extra))
+    args = sys.argv[1:]
+    out = None
+    if len(args) >= 2 and args[0] == "--out":
+        out, args = args[1], args[2:]
+    print(build(verbose=True, extra=args, out_dir=out))

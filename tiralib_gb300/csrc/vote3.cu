@@ -148,7 +148,72 @@ __device__ __forceinline__ void kahan_add(float& sum, float& comp, float x) {
     sum = t;
 }
 
-// one row of voters (fixed vz, oy) against receivers j in [JLO, JHI]
+#ifndef TVGB_FAST_R
+#define TVGB_FAST_R 4          // receivers per thread along z
+#endif
+#ifndef TVGB_FAST_MINB
+#define TVGB_FAST_MINB 2       // resident CTAs per SM the register budget is sized for
+#endif
+
+// one (receiver, voter) pair: stick + closed-form plate (+ ball) into P[0..6]
+template <bool STICK, bool PLATE, bool BALL>
+__device__ __forceinline__ void vote_pair(const float4& A, const float4& B, float lb, float ub, float vb, float oxf,
+                                          float oyf, float oz, const float4& ta, const float4& tb, float* P) {
+    if (STICK) {
+        // stickvote3_accumulate_kernel (tensorvote.h:1184) with power = 1
+        const float u = fmaf(A.z, oz, ub);             // q . o
+        const float k = u * ta.z;                       // 2 (q.o) / |o|^2
+        const float rx = fmaf(-k, oxf, A.x);            // r = q - 2 (q.d) d
+        const float ry = fmaf(-k, oyf, A.y);
+        const float rz = fmaf(-k, oz, A.z);
+        const float eta = fmaf(ta.y, u * u, ta.x);      // c1 + (c2 - c1) (q.d)^2
+        const float term = A.w * eta;
+        const float t0 = term * rx, t1 = term * ry, t2 = term * rz;
+        P[0] = fmaf(t0, rx, P[0]);
+        P[1] = fmaf(t0, ry, P[1]);
+        P[2] = fmaf(t0, rz, P[2]);
+        P[3] = fmaf(t1, ry, P[3]);
+        P[4] = fmaf(t1, rz, P[4]);
+        P[5] = fmaf(t2, rz, P[5]);
+    }
+    if (PLATE) {
+        const float v = fmaf(B.z, oz, vb);             // n . o
+        const float k = v * ta.z;
+        const float mx = fmaf(-k, oxf, B.x);            // m = R n
+        const float my = fmaf(-k, oyf, B.y);
+        const float mz = fmaf(-k, oz, B.z);
+        const float hx = fmaf(v, mx, oxf);              // h = o + v m = -|o| R p
+        const float hy = fmaf(v, my, oyf);
+        const float hz = fmaf(v, mz, oz);
+        const float cA = fmaf(-tb.x, v * v, ta.w);      // c1/2 + (c2 - c1) |p|^2 / 8
+        const float sA = B.w * cA;
+        const float sB = B.w * tb.y;                    // (c2 - c1) / (4 |o|^2)
+        P[6] += sA;
+        const float ax = sA * mx, ay = sA * my, az = sA * mz;
+        const float bx = sB * hx, by = sB * hy, bz = sB * hz;
+        P[0] = fmaf(bx, hx, fmaf(-ax, mx, P[0]));
+        P[1] = fmaf(bx, hy, fmaf(-ax, my, P[1]));
+        P[2] = fmaf(bx, hz, fmaf(-ax, mz, P[2]));
+        P[3] = fmaf(by, hy, fmaf(-ay, my, P[3]));
+        P[4] = fmaf(by, hz, fmaf(-ay, mz, P[4]));
+        P[5] = fmaf(bz, hz, fmaf(-az, mz, P[5]));
+    }
+    if (BALL) {
+        P[6] = fmaf(lb, tb.z, P[6]);
+        const float wb = lb * tb.w;
+        const float wx = wb * oxf, wy = wb * oyf, wz = wb * oz;
+        P[0] = fmaf(wx, oxf, P[0]);
+        P[1] = fmaf(wx, oyf, P[1]);
+        P[2] = fmaf(wx, oz, P[2]);
+        P[3] = fmaf(wy, oyf, P[3]);
+        P[4] = fmaf(wy, oz, P[4]);
+        P[5] = fmaf(wz, oz, P[5]);
+    }
+}
+
+// one row of voters (fixed vz, oy) against receivers j in [JLO, JHI].  The
+// weights depend on ox^2 only, so the voters at +ox and -ox are taken together
+// and share each table load.  rA / rB / rC point at this thread's ox = 0 voter.
 template <int R, int JLO, int JHI, bool STICK, bool PLATE, bool BALL>
 __device__ __forceinline__ void vote_row(const float4* __restrict__ rA, const float4* __restrict__ rB,
                                          const float* __restrict__ rC, const float4* __restrict__ tbl,
@@ -159,74 +224,35 @@ __device__ __forceinline__ void vote_row(const float4* __restrict__ rA, const fl
     for (int j = 0; j < R; ++j)
 #pragma unroll
         for (int k = 0; k < 7; ++k) P[j][k] = 0.0f;
-    float oxf = -float(hw);
-    int off = 2 * (hw * hw + L2y);      // table float4 index of |(-hw, oy, 0)|^2
-    int step = 2 * (-2 * hw + 1);       // 2 * (2 ox + 1)
-    const int nx = 2 * hw + 1;
-#pragma unroll 1
-    for (int i = 0; i < nx; ++i) {
-        float4 A, B;
-        float lb = 0.0f;
-        if (STICK) A = rA[i];
-        if (PLATE) B = rB[i];
-        if (BALL) lb = rC[i];
-        const float ub = STICK ? fmaf(A.x, oxf, A.y * oyf) : 0.0f;
-        const float vb = PLATE ? fmaf(B.x, oxf, B.y * oyf) : 0.0f;
+    const float4 Z4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    {   // ox = 0
+        const float4 A = STICK ? rA[0] : Z4, B = PLATE ? rB[0] : Z4;
+        const float lb = BALL ? rC[0] : 0.0f;
+        const float ub = A.y * oyf, vb = B.y * oyf;
+        const int off = 2 * L2y;
 #pragma unroll
         for (int j = JLO; j <= JHI; ++j) {
             const float4 ta = tbl[zoff[j] + off];
-            const float4 tb = (PLATE || BALL) ? tbl[zoff[j] + off + 1] : make_float4(0, 0, 0, 0);
-            const float oz = ozf[j];
-            if (STICK) {
-                // stickvote3_accumulate_kernel (tensorvote.h:1184) with power = 1
-                const float u = fmaf(A.z, oz, ub);             // q . o
-                const float k = u * ta.z;                       // 2 (q.d) / |o| ... times |o|: 2 u g
-                const float rx = fmaf(-k, oxf, A.x);
-                const float ry = fmaf(-k, oyf, A.y);
-                const float rz = fmaf(-k, oz, A.z);
-                const float eta = fmaf(ta.y, u * u, ta.x);      // c1 + ct (q.d)^2
-                const float term = A.w * eta;
-                const float t0 = term * rx, t1 = term * ry, t2 = term * rz;
-                P[j][0] = fmaf(t0, rx, P[j][0]);
-                P[j][1] = fmaf(t0, ry, P[j][1]);
-                P[j][2] = fmaf(t0, rz, P[j][2]);
-                P[j][3] = fmaf(t1, ry, P[j][3]);
-                P[j][4] = fmaf(t1, rz, P[j][4]);
-                P[j][5] = fmaf(t2, rz, P[j][5]);
-            }
-            if (PLATE) {
-                const float v = fmaf(B.z, oz, vb);             // n . o
-                const float k = v * ta.z;
-                const float mx = fmaf(-k, oxf, B.x);
-                const float my = fmaf(-k, oyf, B.y);
-                const float mz = fmaf(-k, oz, B.z);
-                const float hx = fmaf(v, mx, oxf);
-                const float hy = fmaf(v, my, oyf);
-                const float hz = fmaf(v, mz, oz);
-                const float cA = fmaf(-tb.x, v * v, ta.w);      // c1/2 + ct |p|^2 / 8
-                const float sA = B.w * cA;
-                const float sB = B.w * tb.y;                    // ct g / 4
-                P[j][6] += sA;
-                const float ax = sA * mx, ay = sA * my, az = sA * mz;
-                const float bx = sB * hx, by = sB * hy, bz = sB * hz;
-                P[j][0] = fmaf(bx, hx, fmaf(-ax, mx, P[j][0]));
-                P[j][1] = fmaf(bx, hy, fmaf(-ax, my, P[j][1]));
-                P[j][2] = fmaf(bx, hz, fmaf(-ax, mz, P[j][2]));
-                P[j][3] = fmaf(by, hy, fmaf(-ay, my, P[j][3]));
-                P[j][4] = fmaf(by, hz, fmaf(-ay, mz, P[j][4]));
-                P[j][5] = fmaf(bz, hz, fmaf(-az, mz, P[j][5]));
-            }
-            if (BALL) {
-                P[j][6] = fmaf(lb, tb.z, P[j][6]);
-                const float wb = lb * tb.w;
-                const float wx = wb * oxf, wy = wb * oyf, wz = wb * oz;
-                P[j][0] = fmaf(wx, oxf, P[j][0]);
-                P[j][1] = fmaf(wx, oyf, P[j][1]);
-                P[j][2] = fmaf(wx, oz, P[j][2]);
-                P[j][3] = fmaf(wy, oyf, P[j][3]);
-                P[j][4] = fmaf(wy, oz, P[j][4]);
-                P[j][5] = fmaf(wz, oz, P[j][5]);
-            }
+            const float4 tb = (PLATE || BALL) ? tbl[zoff[j] + off + 1] : Z4;
+            vote_pair<STICK, PLATE, BALL>(A, B, lb, ub, vb, 0.0f, oyf, ozf[j], ta, tb, P[j]);
+        }
+    }
+    float oxf = 1.0f;
+    int off = 2 * (1 + L2y);
+    int step = 6;                        // 2 * (2 ox + 1) for ox = 1
+#pragma unroll 1
+    for (int d = 1; d <= hw; ++d) {
+        const float4 Ap = STICK ? rA[d] : Z4, Am = STICK ? rA[-d] : Z4;
+        const float4 Bp = PLATE ? rB[d] : Z4, Bm = PLATE ? rB[-d] : Z4;
+        const float lp = BALL ? rC[d] : 0.0f, lm = BALL ? rC[-d] : 0.0f;
+        const float ubp = fmaf(Ap.x, oxf, Ap.y * oyf), ubm = fmaf(-Am.x, oxf, Am.y * oyf);
+        const float vbp = fmaf(Bp.x, oxf, Bp.y * oyf), vbm = fmaf(-Bm.x, oxf, Bm.y * oyf);
+#pragma unroll
+        for (int j = JLO; j <= JHI; ++j) {
+            const float4 ta = tbl[zoff[j] + off];
+            const float4 tb = (PLATE || BALL) ? tbl[zoff[j] + off + 1] : Z4;
+            vote_pair<STICK, PLATE, BALL>(Ap, Bp, lp, ubp, vbp, oxf, oyf, ozf[j], ta, tb, P[j]);
+            vote_pair<STICK, PLATE, BALL>(Am, Bm, lm, ubm, vbm, -oxf, oyf, ozf[j], ta, tb, P[j]);
         }
         off += step;
         step += 4;
@@ -301,7 +327,7 @@ __device__ __forceinline__ void write_receiver(const FastArgs& a, size_t idx, si
 }
 
 template <int R, bool STICK, bool PLATE, bool BALL>
-__global__ void __launch_bounds__(VX * VY, 2) k_vote3_fast(FastArgs a) {
+__global__ void __launch_bounds__(VX * VY, TVGB_FAST_MINB) k_vote3_fast(FastArgs a) {
     extern __shared__ __align__(16) float4 smem[];
     const int hw = a.hw;
     const int nt = 3 * hw * hw + 1;          // radial table entries
@@ -360,8 +386,11 @@ __global__ void __launch_bounds__(VX * VY, 2) k_vote3_fast(FastArgs a) {
             }
             __syncthreads();
             for (int oy = oy0; oy <= oy1; ++oy) {
+                // a voter row outside the volume only holds zero records: skip it
+                // (threadIdx.y is uniform within a warp, so is this branch)
+                if ((unsigned)(y0 + int(threadIdx.y) + oy) >= (unsigned)s1) continue;
                 const int rr = threadIdx.y + (oy - oy0);
-                const int base = rr * SW + threadIdx.x;   // column of ox = -hw
+                const int base = rr * SW + threadIdx.x + hw;   // column of ox = 0
                 row_dispatch<R, 0, 0, STICK, PLATE, BALL>(jlo, jhi, sA + base, sB + base, sC + base, tbl, zoff, ozf,
                                                           float(oy), oy * oy, hw, tot, cmp);
             }
@@ -601,7 +630,7 @@ static int launch_fast_t(const FastArgs& a, cudaStream_t st) {
     return TVGB_OK;
 }
 
-constexpr int FAST_R = 4;
+constexpr int FAST_R = TVGB_FAST_R;
 
 static size_t fast_smem(int hw, int rows, bool S, bool P, bool B) {
     const int nt = 3 * hw * hw + 1, SW = VX + 2 * hw, SR = VY + rows - 1;
@@ -610,10 +639,11 @@ static size_t fast_smem(int hw, int rows, bool S, bool P, bool B) {
 }
 
 static int launch_fast(FastArgs a, bool S, bool P, bool B, cudaStream_t st) {
-    // rows per stage: the largest count that keeps two CTAs per SM (<= ~100 KB each)
+    // rows per stage: the largest count that keeps TVGB_FAST_MINB CTAs per SM
     const int w = 2 * a.hw + 1;
+    const size_t budget = (TVGB_FAST_MINB >= 3 ? 72 : 100) * 1024;
     int rows = w;
-    while (rows > 1 && fast_smem(a.hw, rows, S, P, B) > 100 * 1024) rows = (rows + 1) / 2;
+    while (rows > 1 && fast_smem(a.hw, rows, S, P, B) > budget) rows = (rows + 1) / 2;
     if (fast_smem(a.hw, rows, S, P, B) > 200 * 1024) {
         set_error("vote window too large for the shared-memory tile (w = %d)", w);
         return TVGB_ERR_UNSUPPORTED;
