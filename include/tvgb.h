@@ -175,6 +175,28 @@ typedef struct tvgb_vote3_params {
 int tvgb_vote3(const float* in, int in_layout, unsigned s0, unsigned s1, unsigned s2, const tvgb_vote3_params* p,
                float* out, int out_layout, float* evals3, float* evecs, int evec_format, void* stream);
 
+/* Allocation-free variant of tvgb_vote3 (no counterpart in the reference).
+ * For callers that must not allocate device memory while they run: code in
+ * a host-side real-time loop or plugin callback where allocation is
+ * forbidden, or processes whose device memory belongs to another allocator.
+ * It calls no cudaMalloc / cudaMallocAsync / cudaFree and allocates nothing
+ * else: its scratch (the per-voxel voter records) is a file-scope device
+ * array of at most 524288 voxels (e.g. 80^3; 18 MiB held by every GPU that
+ * loads the library, until the process exits).  Limits:
+ *   - all arrays are device memory (in, out, evals3, evecs);
+ *   - s0 * s1 * s2 <= 524288, else TVGB_ERR_ARG;
+ *   - TK with power 1 and samples 0 or >= 3 (the fast kernel), no ATV, else
+ *     TVGB_ERR_ARG;
+ *   - the first call on a device looks up the array's device address
+ *     (cudaGetSymbolAddress) and should come before any stream capture;
+ *   - every call shares the one array: calls whose work overlaps on the GPU
+ *     (different streams, or host threads without ordering) race and must be
+ *     serialised by the caller.  Nothing in the array needs zeroing: each
+ *     call overwrites the records it reads. */
+int tvgb_vote3_noalloc(const float* in, int in_layout, unsigned s0, unsigned s1, unsigned s2,
+                       const tvgb_vote3_params* p, float* out, int out_layout, float* evals3, float* evecs,
+                       int evec_format, void* stream);
+
 /* Whole path on one volume: structure tensor (sigma_st, st_mode as
  * tvgb_structure_tensor3) -> TK vote -> fused eigendecomposition.  Outputs
  * as tvgb_vote3; out_dims receives the voted field's (s0', s1', s2'). */

@@ -810,3 +810,105 @@ int tvgb_tensorvote3(const float* input_field, float* output_field, unsigned s0,
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------ allocation-free 3D vote
+// tvgb_vote3_noalloc: the same preparation and fast vote kernels as tvgb_vote3,
+// for callers that may not allocate device memory while they run -- code
+// inside a host-side real-time loop or plugin callback that forbids
+// allocation, or a process whose device memory is owned by another
+// allocator.  The per-voxel voter records (the only scratch this path uses)
+// live in the file-scope arrays below instead of stream-ordered
+// allocations: every GPU that loads the library holds them until exit.
+#include <mutex>
+
+namespace tvgb {
+
+constexpr size_t NOALLOC_MAX_VOXELS = size_t(1) << 19;   // 524288 voxels (e.g. 80^3): 18 MiB per GPU
+
+static __device__ __align__(256) float4 g_noalloc_stick[NOALLOC_MAX_VOXELS];
+static __device__ __align__(256) float4 g_noalloc_plate[NOALLOC_MAX_VOXELS];
+static __device__ __align__(256) float g_noalloc_ball[NOALLOC_MAX_VOXELS];
+
+struct NoallocScratch {
+    float4* stick;
+    float4* plate;
+    float* ball;
+};
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+static std::mutex g_noalloc_mu;
+static bool g_noalloc_ready[NOALLOC_MAX_DEVICES];
+static NoallocScratch g_noalloc_addr[NOALLOC_MAX_DEVICES];
+
+// Device addresses of the arrays on the current device, looked up once per
+// device (the array names are host-side stand-ins in host code).
+static int noalloc_scratch(NoallocScratch& s) {
+    int dev = 0;
+    TVGB_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) {
+        set_error("tvgb_vote3_noalloc: device %d beyond the supported %d", dev, NOALLOC_MAX_DEVICES);
+        return TVGB_ERR_UNSUPPORTED;
+    }
+    std::lock_guard<std::mutex> g(g_noalloc_mu);
+    if (!g_noalloc_ready[dev]) {
+        NoallocScratch a{};
+        TVGB_CUDA(cudaGetSymbolAddress(reinterpret_cast<void**>(&a.stick), g_noalloc_stick));
+        TVGB_CUDA(cudaGetSymbolAddress(reinterpret_cast<void**>(&a.plate), g_noalloc_plate));
+        TVGB_CUDA(cudaGetSymbolAddress(reinterpret_cast<void**>(&a.ball), g_noalloc_ball));
+        g_noalloc_addr[dev] = a;
+        g_noalloc_ready[dev] = true;
+    }
+    s = g_noalloc_addr[dev];
+    return TVGB_OK;
+}
+
+}  // namespace tvgb
+
+extern "C" int tvgb_vote3_noalloc(const float* in, int in_layout, unsigned s0, unsigned s1, unsigned s2,
+                                  const tvgb_vote3_params* p, float* out, int out_layout, float* evals3, float* evecs,
+                                  int evec_format, void* stream) {
+    TVGB_TRY(check_params(p, "tvgb_vote3_noalloc"));
+    TVGB_CHECK_ARG(in_layout == TVGB_LAYOUT_MAT3 || in_layout == TVGB_LAYOUT_SYM6 || in_layout == TVGB_LAYOUT_SYM6_PLANES,
+                   "tvgb_vote3_noalloc: in_layout must be 9, 6 or 60");
+    TVGB_CHECK_ARG(out_layout == TVGB_LAYOUT_MAT3 || out_layout == TVGB_LAYOUT_SYM6 || out_layout == TVGB_LAYOUT_SYM6_PLANES,
+                   "tvgb_vote3_noalloc: out_layout must be 9, 6 or 60");
+    TVGB_CHECK_ARG(evec_format >= 0 && evec_format <= 2, "tvgb_vote3_noalloc: evec_format must be 0, 1 or 2");
+    const size_t n = size_t(s0) * s1 * s2;
+    if (n == 0) return TVGB_OK;
+    TVGB_CHECK_ARG(n <= NOALLOC_MAX_VOXELS,
+                   "tvgb_vote3_noalloc: %zu voxels exceed the maximum of %zu (use tvgb_vote3 for larger volumes)",
+                   n, NOALLOC_MAX_VOXELS);
+    TVGB_CHECK_ARG(!p->is_atv, "tvgb_vote3_noalloc: ATV is not available without allocation (use tvgb_vote3)");
+    const unsigned power = p->power < 1 ? 1 : p->power;
+    TVGB_CHECK_ARG(power == 1 && (!p->plate || p->samples == 0 || p->samples >= 3),
+                   "tvgb_vote3_noalloc: only power 1 with an exact plate (samples 0 or >= 3) runs without "
+                   "allocation (use tvgb_vote3)");
+    // the caller passes device arrays: staging host memory would allocate
+    TVGB_CHECK_ARG(in && is_device_ptr(in), "tvgb_vote3_noalloc: input must be device memory");
+    TVGB_CHECK_ARG(!out || is_device_ptr(out), "tvgb_vote3_noalloc: out must be device memory");
+    TVGB_CHECK_ARG(!evals3 || is_device_ptr(evals3), "tvgb_vote3_noalloc: evals3 must be device memory");
+    TVGB_CHECK_ARG(!evecs || !evec_format || is_device_ptr(evecs), "tvgb_vote3_noalloc: evecs must be device memory");
+    NoallocScratch sc;
+    TVGB_TRY(noalloc_scratch(sc));
+    cudaStream_t st = as_stream(stream);
+    const bool S = p->stick != 0, P = p->plate != 0, B = p->ball != 0;
+    const unsigned w = p->w ? p->w : auto_window(p->sigma1, p->sigma2);
+    PrepOut po{};
+    po.A = S ? sc.stick : nullptr;
+    po.B = P ? sc.plate : nullptr;
+    po.C = B ? sc.ball : nullptr;
+    const float sn = S ? 1.0f / sticknorm3_f(p->sigma1, p->sigma2, power) : 1.0f;
+    TVGB_TRY(launch_prep(in, in_layout, n, po, sn, p->parity, st));
+    FastArgs fa{};
+    fa.A = po.A; fa.B = po.B; fa.C = po.C;
+    fa.s0 = int(s0); fa.s1 = int(s1); fa.s2 = int(s2); fa.hw = int(w / 2);
+    fa.sig1 = p->sigma1; fa.sig2 = p->sigma2;
+    fa.out = out; fa.out_layout = out_layout; fa.evals = evals3;
+    fa.evecs = evec_format ? evecs : nullptr; fa.evec_fmt = evec_format;
+    fa.precise_eig = p->parity ? 0 : 1;
+    if (!S && !P && !B) {
+        if (out) TVGB_CUDA(cudaMemsetAsync(out, 0, n * (out_layout == TVGB_LAYOUT_MAT3 ? 36 : 24), st));
+        return TVGB_OK;
+    }
+    return launch_fast(fa, S, P, B, st);
+}
