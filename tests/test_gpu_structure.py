@@ -44,6 +44,19 @@ def test_structure_tensor3_matches_oracle(tv, mode, shape, sigma):
     assert rel(out, ref) < 1e-5
 
 
+# every fixed-tap kernel (K = 3 .. 13) and the any-K kernel (K = 15, 25);
+# deep volumes so that several z chunks meet inside the volume
+@pytest.mark.parametrize("sigma", [0.3, 0.7, 1.7, 2.5, 4.0])
+@pytest.mark.parametrize("mode", ["valid", "same"])
+def test_structure_tensor3_tap_counts(tv, sigma, mode):
+    rng = np.random.default_rng(int(sigma * 10))
+    v = rng.normal(size=(90, 37, 45)).astype(np.float32)
+    out = tv.structure_tensor3(v, sigma, mode=mode, layout="planes")
+    ref = O.structure_tensor3(v, sigma, 0 if mode == "valid" else 1)
+    assert out.shape == ref.shape
+    assert rel(out, ref) < 1e-5
+
+
 def test_structure_tensor3_layouts_agree(tv):
     rng = np.random.default_rng(1)
     v = rng.normal(size=(12, 13, 14)).astype(np.float32)

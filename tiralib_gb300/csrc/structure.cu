@@ -8,12 +8,14 @@
 // memory, intermediates in HBM and a device synchronise after each pass.
 //
 // Here one kernel does it all: a CTA owns a 32 x 8 output column and marches
-// through the input z-planes; per plane it forms the gradient (central
-// inside, one-sided at the faces), the six products on the haloed xy region,
-// blurs them along x and y in shared memory, and keeps the last K xy-blurred
-// planes in a shared-memory ring from which each finished output plane is
-// blurred along z and written once.  HBM traffic ~ one read of the volume
-// plus one write of the six components (28 B per voxel).
+// through the input z-planes, keeping the last three raw planes (with a
+// one-voxel halo) in shared memory so each input value is read from HBM about
+// once; per plane it forms the gradient (central inside, one-sided at the
+// faces), the six products on the haloed xy region, blurs them along y then x
+// in shared memory, and keeps the last K blurred planes in a shared-memory
+// ring from which each finished output plane is blurred along z and written
+// once.  HBM traffic ~ one read of the volume plus one write of the six
+// components (28 B per voxel).
 //
 // tvgb_gaussian_filter3d / tvgb_gaussian_convolve2 keep the reference's
 // scalar, valid-convolution contract (filter.h:401, :305) with a coalesced
@@ -65,10 +67,6 @@ struct StArgs {
     int layout;
 };
 
-__device__ __forceinline__ float vol_at(const StArgs& a, int z, int y, int x) {
-    return __ldg(a.vol + (size_t(z) * a.s1 + y) * a.s2 + x);
-}
-
 // d/d(axis) at an in-volume voxel: volume<T>::gradient's rule
 __device__ __forceinline__ float grad1(float lo, float c, float hi, int p, int S) {
     if (S < 2) return 0.0f;
@@ -77,65 +75,93 @@ __device__ __forceinline__ float grad1(float lo, float c, float hi, int p, int S
     return (hi - lo) * 0.5f;
 }
 
-__global__ void __launch_bounds__(STX * STY) k_st3(StArgs a) {
+// Shared memory (floats), with EX = 32 + K - 1, EY = 8 + K - 1:
+//   raw   3 x (EY + 2) x (EX + 2)   input planes iz-1, iz, iz+1 (ring by plane index mod 3)
+//   sT    6 x EY x EX               gradient products of plane iz on the haloed region
+//   sY    6 x 8 x EX                blurred along y
+//   ring  K x 6 x 8 x 32            blurred along y and x, last K planes
+__global__ void __launch_bounds__(STX * STY) k_st3_any(StArgs a) {
     extern __shared__ __align__(16) float sm[];
     const int K = a.K;
     const int EX = STX + K - 1, EY = STY + K - 1;
-    float* sT = sm;                          // 6 x EY x EX products
-    float* sX = sT + 6 * EY * EX;            // 6 x EY x STX x-blurred
-    float* ring = sX + 6 * EY * STX;         // K x 6 x STY x STX xy-blurred
+    const int RX = EX + 2, RY = EY + 2;
+    float* raw = sm;
+    float* sT = raw + 3 * RY * RX;
+    float* sY = sT + 6 * EY * EX;
+    float* ring = sY + 6 * STY * EX;
     __shared__ float g[MAXK];
     const int tid = threadIdx.y * STX + threadIdx.x;
+    const int nthr = STX * STY;
     if (tid < K) g[tid] = a.g[tid];
 
     const int ox0 = blockIdx.x * STX, oy0 = blockIdx.y * STY;
     const int oz_lo = blockIdx.z * a.zchunk, oz_hi = min(a.o0 - 1, oz_lo + a.zchunk - 1);
-    // input z-planes feeding outputs [oz_lo, oz_hi]: iz = oz + c - off, c in [0, K)
-    const int iz_lo = oz_lo - a.off, iz_hi = oz_hi + K - 1 - a.off;
-    const int ix0 = ox0 - a.off, iy0 = oy0 - a.off;   // input coords of region origin
+    const int iz_lo = oz_lo - a.off, iz_hi = oz_hi + K - 1 - a.off;   // input planes feeding [oz_lo, oz_hi]
+    const int ix0 = ox0 - a.off, iy0 = oy0 - a.off;                     // input coords of the product region
     const size_t on = size_t(a.o0) * a.o1 * a.o2;
 
+    // raw plane p -> slot, region x in [ix0 - 1, ix0 + EX], y in [iy0 - 1, iy0 + EY]
+    auto load_raw = [&](int p) {
+        float* dst = raw + (((p % 3) + 3) % 3) * RY * RX;
+        const bool zin = p >= 0 && p < a.s0;
+        for (int e = tid; e < RY * RX; e += nthr) {
+            const int ry = e / RX, rx = e - ry * RX;
+            const int x = ix0 - 1 + rx, y = iy0 - 1 + ry;
+            float v = 0.0f;
+            if (zin && (unsigned)x < (unsigned)a.s2 && (unsigned)y < (unsigned)a.s1)
+                v = __ldg(a.vol + (size_t(p) * a.s1 + y) * a.s2 + x);
+            dst[e] = v;
+        }
+    };
+    load_raw(iz_lo - 1);
+    load_raw(iz_lo);
     for (int iz = iz_lo; iz <= iz_hi; ++iz) {
-        const bool zin = iz >= 0 && iz < a.s0;
-        // (b) products on the haloed region
-        for (int e = tid; e < EY * EX; e += STX * STY) {
-            const int ry = e / EX, rx = e - ry * EX;
-            const int x = ix0 + rx, y = iy0 + ry;
-            float gx = 0.0f, gy = 0.0f, gz = 0.0f;
-            if (zin && x >= 0 && x < a.s2 && y >= 0 && y < a.s1) {
-                const float c = vol_at(a, iz, y, x);
-                const float xl = x > 0 ? vol_at(a, iz, y, x - 1) : c, xh = x + 1 < a.s2 ? vol_at(a, iz, y, x + 1) : c;
-                const float yl = y > 0 ? vol_at(a, iz, y - 1, x) : c, yh = y + 1 < a.s1 ? vol_at(a, iz, y + 1, x) : c;
-                const float zl = iz > 0 ? vol_at(a, iz - 1, y, x) : c, zh = iz + 1 < a.s0 ? vol_at(a, iz + 1, y, x) : c;
-                gx = grad1(xl, c, xh, x, a.s2);
-                gy = grad1(yl, c, yh, y, a.s1);
-                gz = grad1(zl, c, zh, iz, a.s0);
-            }
+        load_raw(iz + 1);
+        __syncthreads();
+        // gradient products on the haloed region (zero outside the volume)
+        {
+            const float* R0 = raw + ((((iz - 1) % 3) + 3) % 3) * RY * RX;
+            const float* R1 = raw + (((iz % 3) + 3) % 3) * RY * RX;
+            const float* R2 = raw + ((((iz + 1) % 3) + 3) % 3) * RY * RX;
+            const bool zin = iz >= 0 && iz < a.s0;
             const int ps = EY * EX;
-            sT[e] = gx * gx; sT[ps + e] = gx * gy; sT[2 * ps + e] = gx * gz;
-            sT[3 * ps + e] = gy * gy; sT[4 * ps + e] = gy * gz; sT[5 * ps + e] = gz * gz;
+            for (int e = tid; e < ps; e += nthr) {
+                const int ry = e / EX, rx = e - ry * EX;
+                const int x = ix0 + rx, y = iy0 + ry;
+                float gx = 0.0f, gy = 0.0f, gz = 0.0f;
+                if (zin && (unsigned)x < (unsigned)a.s2 && (unsigned)y < (unsigned)a.s1) {
+                    const int c = (ry + 1) * RX + rx + 1;
+                    gx = grad1(R1[c - 1], R1[c], R1[c + 1], x, a.s2);
+                    gy = grad1(R1[c - RX], R1[c], R1[c + RX], y, a.s1);
+                    gz = grad1(R0[c], R1[c], R2[c], iz, a.s0);
+                }
+                sT[e] = gx * gx; sT[ps + e] = gx * gy; sT[2 * ps + e] = gx * gz;
+                sT[3 * ps + e] = gy * gy; sT[4 * ps + e] = gy * gz; sT[5 * ps + e] = gz * gz;
+            }
         }
         __syncthreads();
-        // (c) blur along x: sX[c][ry][tx]
-        for (int e = tid; e < 6 * EY * STX; e += STX * STY) {
-            const int c = e / (EY * STX), r = e - c * EY * STX, ry = r / STX, tx = r - ry * STX;
-            const float* src = sT + c * EY * EX + ry * EX + tx;
-            float s = 0.0f;
-            for (int k = 0; k < K; ++k) s = fmaf(g[k], src[k], s);
-            sX[e] = s;
+        // blur along y: sY[c][ty][rx]
+        for (int e = tid; e < 6 * STY * EX; e += nthr) {
+            const int c = e / (STY * EX), r = e - c * STY * EX, ty = r / EX, rx = r - ty * EX;
+            const float* src = sT + c * EY * EX + ty * EX + rx;
+            float sacc = 0.0f;
+            for (int k = 0; k < K; ++k) sacc = fmaf(g[k], src[k * EX], sacc);
+            sY[e] = sacc;
         }
         __syncthreads();
-        // (d) blur along y into the ring slot of this plane
-        float* slot = ring + ((iz - iz_lo) % K) * 6 * STY * STX;
-        for (int e = tid; e < 6 * STY * STX; e += STX * STY) {
-            const int c = e / (STY * STX), r = e - c * STY * STX, ty = r / STX, tx = r - ty * STX;
-            const float* src = sX + c * EY * STX + ty * STX + tx;
-            float s = 0.0f;
-            for (int k = 0; k < K; ++k) s = fmaf(g[k], src[k * STX], s);
-            slot[e] = s;
+        // blur along x into the ring slot of this plane
+        {
+            float* slot = ring + ((iz - iz_lo) % K) * 6 * STY * STX;
+            for (int e = tid; e < 6 * STY * STX; e += nthr) {
+                const int c = e / (STY * STX), r = e - c * STY * STX, ty = r / STX, tx = r - ty * STX;
+                const float* src = sY + c * STY * EX + ty * EX + tx;
+                float sacc = 0.0f;
+                for (int k = 0; k < K; ++k) sacc = fmaf(g[k], src[k], sacc);
+                slot[e] = sacc;
+            }
         }
         __syncthreads();
-        // (e) output plane oz = iz - (K - 1) + off is complete
+        // output plane oz = iz - (K - 1) + off is complete: blur along z and write
         const int oz = iz - (K - 1) + a.off;
         if (oz >= oz_lo && oz <= oz_hi) {
             const int x = ox0 + threadIdx.x, y = oy0 + threadIdx.y;
@@ -158,9 +184,190 @@ __global__ void __launch_bounds__(STX * STY) k_st3(StArgs a) {
                 }
             }
         }
-        // the next plane's step (b) overwrites sT only; the ring slot it later
-        // writes is not read by (e) of this iteration after this barrier
-        __syncthreads();
+        // the next iteration's raw load writes the slot of plane iz - 1, last
+        // read before the barrier that follows the products; its ring write
+        // (slot of plane iz + 1 - K, read just above) comes after two barriers
+    }
+}
+
+// Fixed-K variant (odd K <= ST_MAXT).  Same arithmetic, reorganised so that
+// each shared-memory value feeds several FMAs:
+//   * y blur: one thread per (channel, haloed column) computes the tile's 8
+//     rows from one pass down the column, kept in registers;
+//   * x blur: one thread per (channel triple, row, pair of x) reads its row
+//     segment with 64-bit loads and produces both outputs;
+//   * z blur: each thread keeps, for its 6 outputs, the K partial sums of the
+//     planes in flight in registers; slot (plane mod K) is resolved by a
+//     warp-uniform dispatch so every index is static;
+//   * the next raw plane is fetched into registers before the products and
+//     stored after them, so its global latency overlaps two stages.
+constexpr int ST_MAXT = 13;
+
+template <int K, int J>
+__device__ __forceinline__ void st_zstep(float (&acc)[6][K], const float (&v)[6], const float (&gw)[K],
+                                         float (&done)[6]) {
+#pragma unroll
+    for (int m = 0; m < K; ++m) {
+        const int sl = (J - m + K) % K;
+#pragma unroll
+        for (int o = 0; o < 6; ++o) acc[o][sl] = fmaf(gw[m], v[o], acc[o][sl]);
+    }
+    constexpr int sd = (J + 1) % K;
+#pragma unroll
+    for (int o = 0; o < 6; ++o) { done[o] = acc[o][sd]; acc[o][sd] = 0.0f; }
+}
+
+template <int K, int J = 0>
+__device__ __forceinline__ void st_zdispatch(int j, float (&acc)[6][K], const float (&v)[6], const float (&gw)[K],
+                                             float (&done)[6]) {
+    if constexpr (J < K) {
+        if (j == J) st_zstep<K, J>(acc, v, gw, done);
+        else st_zdispatch<K, J + 1>(j, acc, v, gw, done);
+    }
+}
+
+template <int K>
+__global__ void __launch_bounds__(STX * STY, 2) k_st3(StArgs a) {
+    constexpr int EX = STX + K - 1, EY = STY + K - 1;   // EX even: 64-bit row loads stay aligned
+    constexpr int RX = EX + 2, RY = EY + 2;
+    constexpr int NT = STX * STY;
+    constexpr int NR = (RY * RX + NT - 1) / NT;          // raw elements per thread per plane
+    __shared__ __align__(16) float raw[3 * RY * RX];
+    __shared__ __align__(16) float sT[6 * EY * EX];
+    __shared__ __align__(16) float sY[6 * STY * EX];
+    const int tid = threadIdx.x;
+    float gw[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) gw[k] = a.g[k];
+
+    const int ox0 = blockIdx.x * STX, oy0 = blockIdx.y * STY;
+    const int oz_lo = blockIdx.z * a.zchunk, oz_hi = min(a.o0 - 1, oz_lo + a.zchunk - 1);
+    const int iz_lo = oz_lo - a.off, iz_hi = oz_hi + K - 1 - a.off;
+    const int ix0 = ox0 - a.off, iy0 = oy0 - a.off;
+    const size_t on = size_t(a.o0) * a.o1 * a.o2;
+
+    // owned outputs: channels 3h..3h+2 at (x0 + {0,1}, y) of every plane
+    const int h = tid >> 7, ty = (tid >> 4) & 7, px = (tid & 15) * 2;
+    const int y = oy0 + ty, x0 = ox0 + px;
+
+    float pre[NR];
+    auto fetch = [&](int p) {
+        const bool zin = p >= 0 && p < a.s0;
+#pragma unroll
+        for (int r = 0; r < NR; ++r) {
+            const int e = tid + r * NT;
+            const int ry = e / RX, rx = e - ry * RX;
+            const int gx = ix0 - 1 + rx, gy = iy0 - 1 + ry;
+            pre[r] = (e < RY * RX && zin && (unsigned)gx < (unsigned)a.s2 && (unsigned)gy < (unsigned)a.s1)
+                         ? __ldg(a.vol + (size_t(p) * a.s1 + gy) * a.s2 + gx)
+                         : 0.0f;
+        }
+    };
+    auto store = [&](int p) {
+        float* dst = raw + (((p % 3) + 3) % 3) * RY * RX;
+#pragma unroll
+        for (int r = 0; r < NR; ++r) {
+            const int e = tid + r * NT;
+            if (e < RY * RX) dst[e] = pre[r];
+        }
+    };
+    fetch(iz_lo - 1); store(iz_lo - 1);
+    fetch(iz_lo); store(iz_lo);
+    fetch(iz_lo + 1); store(iz_lo + 1);
+
+    float acc[6][K];
+#pragma unroll
+    for (int o = 0; o < 6; ++o)
+#pragma unroll
+        for (int k = 0; k < K; ++k) acc[o][k] = 0.0f;
+
+    for (int iz = iz_lo; iz <= iz_hi; ++iz) {
+        const bool zin = iz >= 0 && iz < a.s0;
+        fetch(iz + 2);
+        __syncthreads();   // raw plane iz + 1 stored; previous x blur done with sY
+        if (zin) {
+            const float* R0 = raw + ((((iz - 1) % 3) + 3) % 3) * RY * RX;
+            const float* R1 = raw + (((iz % 3) + 3) % 3) * RY * RX;
+            const float* R2 = raw + ((((iz + 1) % 3) + 3) % 3) * RY * RX;
+            constexpr int ps = EY * EX;
+            for (int e = tid; e < ps; e += NT) {
+                const int ry = e / EX, rx = e - ry * EX;
+                const int gxp = ix0 + rx, gyp = iy0 + ry;
+                float gx = 0.0f, gy = 0.0f, gz = 0.0f;
+                if ((unsigned)gxp < (unsigned)a.s2 && (unsigned)gyp < (unsigned)a.s1) {
+                    const int c = (ry + 1) * RX + rx + 1;
+                    gx = grad1(R1[c - 1], R1[c], R1[c + 1], gxp, a.s2);
+                    gy = grad1(R1[c - RX], R1[c], R1[c + RX], gyp, a.s1);
+                    gz = grad1(R0[c], R1[c], R2[c], iz, a.s0);
+                }
+                sT[e] = gx * gx; sT[ps + e] = gx * gy; sT[2 * ps + e] = gx * gz;
+                sT[3 * ps + e] = gy * gy; sT[4 * ps + e] = gy * gz; sT[5 * ps + e] = gz * gz;
+            }
+        }
+        __syncthreads();   // products ready; raw plane iz - 1 no longer read
+        store(iz + 2);
+        if (zin) {
+            for (int it = tid; it < 6 * EX; it += NT) {
+                const int c = it / EX, rx = it - c * EX;
+                const float* col = sT + c * EY * EX + rx;
+                float cv[EY];
+#pragma unroll
+                for (int r = 0; r < EY; ++r) cv[r] = col[r * EX];
+#pragma unroll
+                for (int t = 0; t < STY; ++t) {
+                    float s = 0.0f;
+#pragma unroll
+                    for (int k = 0; k < K; ++k) s = fmaf(gw[k], cv[t + k], s);
+                    sY[(c * STY + t) * EX + rx] = s;
+                }
+            }
+        }
+        __syncthreads();   // y blur ready
+        float v[6];
+        if (zin) {
+#pragma unroll
+            for (int cc = 0; cc < 3; ++cc) {
+                const float2* row = reinterpret_cast<const float2*>(sY + ((3 * h + cc) * STY + ty) * EX + px);
+                float s0 = 0.0f, s1 = 0.0f;
+#pragma unroll
+                for (int q = 0; q < (K + 1) / 2; ++q) {
+                    const float2 u = row[q];
+                    // u.x = sY[px + 2q], u.y = sY[px + 2q + 1]
+                    if (2 * q < K) s0 = fmaf(gw[2 * q], u.x, s0);
+                    if (2 * q + 1 < K) s0 = fmaf(gw[2 * q + 1], u.y, s0);
+                    if (2 * q >= 1) s1 = fmaf(gw[2 * q - 1], u.x, s1);
+                    s1 = fmaf(gw[2 * q], u.y, s1);
+                }
+                v[2 * cc] = s0; v[2 * cc + 1] = s1;
+            }
+        } else {
+#pragma unroll
+            for (int o = 0; o < 6; ++o) v[o] = 0.0f;
+        }
+        float done[6];
+        st_zdispatch<K>((iz - iz_lo) % K, acc, v, gw, done);
+        // the slot just completed began at plane iz - K + 1: output oz
+        const int oz = iz - (K - 1) + a.off;
+        if (oz >= oz_lo && y < a.o1) {
+            const size_t row0 = (size_t(oz) * a.o1 + y) * a.o2;
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                const int x = x0 + u;
+                if (x >= a.o2) continue;
+                const size_t idx = row0 + x;
+                const float c0 = done[u], c1 = done[2 + u], c2 = done[4 + u];   // channels 3h, 3h+1, 3h+2
+                if (a.layout == TVGB_LAYOUT_SYM6_PLANES) {
+                    a.out[(3 * h) * on + idx] = c0; a.out[(3 * h + 1) * on + idx] = c1; a.out[(3 * h + 2) * on + idx] = c2;
+                } else if (a.layout == TVGB_LAYOUT_SYM6) {
+                    float* o = a.out + idx * 6 + 3 * h;
+                    o[0] = c0; o[1] = c1; o[2] = c2;
+                } else {
+                    float* o = a.out + idx * 9;
+                    if (h == 0) { o[0] = c0; o[1] = c1; o[3] = c1; o[2] = c2; o[6] = c2; }
+                    else { o[4] = c0; o[5] = c1; o[7] = c1; o[8] = c2; }
+                }
+            }
+        }
     }
 }
 
@@ -190,18 +397,50 @@ int structure_tensor3_device(const float* vol, unsigned s0, unsigned s1, unsigne
     gaussian1d(K, sigma, a.g);
     a.out = out; a.layout = out_layout;
     const unsigned gx = ceil_div(d[2], STX), gy = ceil_div(d[1], STY);
-    // enough CTAs for ~4 waves on 152 SMs, but chunks long enough to amortise the K-1 plane ramp
-    int zchunk = int(d[0]);
-    const size_t target = 152 * 8;
-    while (zchunk > 4 * int(K) && size_t(gx) * gy * ceil_div(d[0], unsigned(zchunk)) < target) zchunk = (zchunk + 1) / 2;
-    a.zchunk = zchunk;
+    const bool fixed = K <= unsigned(ST_MAXT);
     const int EX = STX + int(K) - 1, EY = STY + int(K) - 1;
-    const size_t smem = sizeof(float) * (size_t(6) * EY * EX + size_t(6) * EY * STX + size_t(K) * 6 * STY * STX);
-    TVGB_CUDA(cudaFuncSetAttribute(k_st3, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    const size_t smem = fixed ? 0
+                              : sizeof(float) * (size_t(3) * (EY + 2) * (EX + 2) + size_t(6) * EY * EX +
+                                                 size_t(6) * STY * EX + size_t(K) * 6 * STY * STX);
+    const void* fn = nullptr;
+    switch (K) {
+        case 3: fn = (const void*)k_st3<3>; break;
+        case 5: fn = (const void*)k_st3<5>; break;
+        case 7: fn = (const void*)k_st3<7>; break;
+        case 9: fn = (const void*)k_st3<9>; break;
+        case 11: fn = (const void*)k_st3<11>; break;
+        case 13: fn = (const void*)k_st3<13>; break;
+        default: fn = (const void*)k_st3_any; break;
+    }
+    if (!fixed) TVGB_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    // z chunk.  Each CTA walks zc + K - 1 planes (K - 1 of them ramp).  Cost
+    // model: the busiest SM's planes, divided by the speed-up of running n
+    // CTAs side by side on one SM (taken as n^0.7, n up to the occupancy).
+    int dev = 0, sms = 0, per_sm = 0;
+    TVGB_CUDA(cudaGetDevice(&dev));
+    TVGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    TVGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, STX * STY, smem));
+    sms = std::max(1, sms);
+    per_sm = std::max(1, per_sm);
+    int zchunk = int(d[0]);
+    double best = 0.0;
+    for (int zc = int(d[0]); zc >= 1; zc = zc > 64 ? zc - zc / 16 : zc - 1) {
+        const size_t ctas = size_t(gx) * gy * ceil_div(d[0], unsigned(zc));
+        const size_t per = (ctas + size_t(sms) - 1) / size_t(sms);
+        const double conc = std::pow(double(std::min(per, size_t(per_sm))), 0.7);
+        const double cost = double(per) * double(zc + int(K) - 1) / conc;
+        if (best == 0.0 || cost < best) { best = cost; zchunk = zc; }
+    }
+    a.zchunk = zchunk;
     dim3 grid(gx, gy, ceil_div(d[0], unsigned(zchunk)));
     {
         KernelTimer kt_("k_st3", st);
-        k_st3<<<grid, dim3(STX, STY), smem, st>>>(a);
+        if (fixed) {
+            void* args[] = {&a};
+            TVGB_CUDA(cudaLaunchKernel(fn, grid, dim3(STX * STY), args, 0, st));
+        } else {
+            k_st3_any<<<grid, dim3(STX, STY), smem, st>>>(a);
+        }
         kt_.stop();
     }
     TVGB_LAUNCHED();
