@@ -26,6 +26,7 @@ per step.  Under torchrun every rank processes its own volume (weak scaling,
 no collective on the data path); the reported time is the max over ranks.
 """
 import argparse
+import ctypes
 import json
 import os
 import subprocess
@@ -359,6 +360,319 @@ def run_ours(args, rank, world, local_rank):
         dist.destroy_process_group()
 
 
+# ----------------------------------------------------------------------------- C3: batched 3x3 eigen
+
+C3_METRIC = "batched 3x3 symmetric eigendecomposition tensors/s (FP32 + FP64 refinement of near-degenerate pairs)"
+
+
+def eigen_batch_gpu(n, seed, dev, chunk=1 << 24):
+    """n float32 tensors Q diag(l) Q^T on the GPU: Q a Haar rotation (random
+    unit quaternion), l log-uniform in [1e-6, 1e3]; 10 % with a pair within
+    1e-6 relative, 1 % fully degenerate (the C3 recipe)."""
+    import torch
+    out = torch.empty((n, 9), device=dev)
+    g = torch.Generator(device=dev).manual_seed(seed)
+    for s in range(0, n, chunk):
+        m = min(chunk, n - s)
+        q = torch.randn((m, 4), device=dev, generator=g, dtype=torch.float64)
+        q = q / q.norm(dim=1, keepdim=True)
+        w, x, y, z = q.unbind(1)
+        Q = torch.stack([1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y),
+                         2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x),
+                         2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)], dim=1).view(m, 3, 3)
+        lam = 10.0 ** (torch.rand((m, 3), device=dev, generator=g, dtype=torch.float64) * 9.0 - 6.0)
+        k = torch.rand(m, device=dev, generator=g, dtype=torch.float64)
+        pair = k < 0.10
+        lam[pair, 1] = lam[pair, 0] * (1 + (torch.rand(int(pair.sum()), device=dev, generator=g,
+                                                       dtype=torch.float64) * 2 - 1) * 1e-6)
+        full = k >= 0.99
+        lam[full, 1] = lam[full, 0]
+        lam[full, 2] = lam[full, 0]
+        M = (Q * lam[:, None, :]) @ Q.transpose(1, 2)
+        out[s:s + m] = M.reshape(m, 9).float()
+    return out
+
+
+def eigen_errors(m9, ev, vec):
+    """Errors against the FP64 oracle (Jacobi on the float32 input):
+    eigenvalues normwise (|dl| / max|l|); eigenvector angle, separately for
+    eigenvalues whose nearest neighbour is > 1e-3 |l_max| away and for those
+    within (1e-9, 1e-3] |l_max| (near-degenerate pairs; the float32 input
+    still determines them); and the backward error ||A V - V L|| / ||A||."""
+    from oracle import oracle as O
+    u = [0, 1, 2, 4, 5, 8]
+    ref_ev, ref_vec = O.eig3_f64(m9[:, u].astype(np.float64))
+    scale = np.abs(ref_ev).max(axis=1, keepdims=True)
+    ev_err = (np.abs(ev - ref_ev) / scale).ravel()
+    gaps = np.diff(ref_ev, axis=1) / scale
+    gmin = np.full(ref_ev.shape, np.inf)           # relative gap to the nearest neighbour
+    gmin[:, :2] = np.minimum(gmin[:, :2], gaps)
+    gmin[:, 1:] = np.minimum(gmin[:, 1:], gaps)
+    sep = gmin > 1e-3
+    near = (gmin > 1e-9) & ~sep
+    v64 = vec.astype(np.float64)
+    v64 = v64 / np.linalg.norm(v64, axis=2, keepdims=True)
+    dot = np.abs(np.einsum("nij,nij->ni", v64, ref_vec))
+    crs = np.linalg.norm(np.cross(v64, ref_vec), axis=2)
+    ang_all = np.arctan2(crs, dot)   # well conditioned at small angles, unlike arccos
+    ang, ang_near = ang_all[sep], ang_all[near]
+    A = m9.reshape(-1, 3, 3).astype(np.float64)
+    V = vec.astype(np.float64)
+    res = np.einsum("nij,nkj->nki", A, V) - ev.astype(np.float64)[:, :, None] * V
+    bw = np.linalg.norm(res.reshape(len(A), -1), axis=1) / np.linalg.norm(A.reshape(len(A), -1), axis=1)
+    stat = lambda x: {"max": float(np.max(x)), "median": float(np.median(x))} if len(x) else None
+    return {"eigenvalue_normwise": stat(ev_err), "eigenvector_angle_rad": stat(ang),
+            "eigenvector_angle_near_degenerate_rad": stat(ang_near), "n_near_degenerate": int(near.sum()),
+            "backward": stat(bw), "n": int(len(m9))}
+
+
+def run_c3(args, rank, world, local_rank):
+    import torch
+    import tiralib_gb300 as tv
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    n = 1 << args.size if args.size else 1 << 27
+    mats = eigen_batch_gpu(n, 3 + rank, dev)
+    ev = torch.empty((n, 3), device=dev)
+    vec = torch.empty((n, 3, 3), device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    lib = tv.lib()
+    buf = ctypes.create_string_buffer(1 << 14)
+
+    def timed(precise):
+        for _ in range(args.warmup):
+            tv.api.call("tvgb_eig3", tv.api._ptr(mats), 9, n, tv.api._ptr(ev), tv.api._ptr(vec), 1, int(precise),
+                        None, tv.api._stream_for(mats))
+        torch.cuda.synchronize()
+        lib.tvgb_profile_enable(1)
+        lib.tvgb_profile_read(buf, len(buf))
+        ts = []
+        l0 = tv.launch_count()
+        for _ in range(args.steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            tv.api.call("tvgb_eig3", tv.api._ptr(mats), 9, n, tv.api._ptr(ev), tv.api._ptr(vec), 1, int(precise),
+                        None, tv.api._stream_for(mats))
+            e1.record()
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        launches = tv.launch_count() - l0
+        lib.tvgb_profile_read(buf, len(buf))
+        lib.tvgb_profile_enable(0)
+        return float(np.sum(ts)) / 1e3, launches, parse_profile(buf.value.decode())
+
+    with ClockSampler(gpu_index_for(local_rank)) as clk:
+        t_precise, launches, prof = timed(True)
+    clocks = clk.summary()
+    t_parity, _, prof_par = timed(False)
+    _, _, nref = tv.eig3(mats[: 1 << 20], precise=True)
+    # precision on a 2^16 sample of the same tensors
+    idx = torch.randperm(n, device=dev, generator=torch.Generator(device=dev).manual_seed(9))[: 1 << 16]
+    m_s = mats[idx].contiguous()
+    ev_p, vec_p, _ = tv.eig3(m_s, precise=True)
+    ev_r, vec_r, _ = tv.eig3(m_s, precise=False)
+    m_h = m_s.cpu().numpy()
+    err_precise = eigen_errors(m_h, ev_p.cpu().numpy(), vec_p.cpu().numpy())
+    err_parity = eigen_errors(m_h, ev_r.cpu().numpy(), vec_r.cpu().numpy())
+    # end to end with pinned host buffers
+    mats_h = mats.cpu().pin_memory()
+    ev_h = torch.empty((n, 3)).pin_memory()
+    vec_h = torch.empty((n, 3, 3)).pin_memory()
+    mn, evn, vecn = mats_h.numpy(), ev_h.numpy(), vec_h.numpy()
+    tv.eig3(mn[:1024], precise=True)
+    e2e = []
+    for _ in range(max(1, min(args.steps, 3))):
+        t0 = time.perf_counter()
+        tv.api.call("tvgb_eig3", tv.api._ptr(mn), 9, n, tv.api._ptr(evn), tv.api._ptr(vecn), 1, 1, None, None)
+        e2e.append(time.perf_counter() - t0)
+    peaks = measured_peaks()
+    nl, tot = prof.get("k_eig3", (0, 0.0))
+    bytes_per = 36 + 12 + 36
+    roof = None
+    if nl:
+        avg = tot / nl / 1e3
+        ach = n * bytes_per / avg / 1e9
+        roof = {"bound": "hbm", "kernel": "k_eig3 (precise)", "achieved": ach, "peak": peaks["hbm_gbs"],
+                "unit": "GB/s", "frac": ach / peaks["hbm_gbs"], "peak_source": peaks["source"],
+                "traffic": profiled_traffic("k_eig3"), "bytes_per_tensor": bytes_per, "avg_launch_ms": avg * 1e3}
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        v, th, desc = cpu_eigen_sample()
+        cpu = {"value": v, "unit": "tensors/s", "cores": th, "kind": "port", "sample": desc}
+    if rank == 0:
+        print(json.dumps({
+            "metric": C3_METRIC, "value": world * args.steps * n / t_precise, "unit": "tensors/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_precise / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 refinement)",
+            "data": "synthetic",
+            "config": {"workload": f"C3: 2^{int(np.log2(n))} tensors Q diag(l) Q^T, Haar Q, l log-uniform [1e-6, 1e3],"
+                                   " 10% near-degenerate pair, 1% fully degenerate; mat3 in, eigenvalues + "
+                                   "cartesian eigenvectors out", "tensors": n,
+                       "l2_flush": "256 MiB write between timed steps (outside the events)"},
+            "parity_mode_tensors_per_s": args.steps * n / t_parity,
+            "fp64_refined_fraction": nref / float(1 << 20),
+            "errors_vs_fp64": {"precise": err_precise, "parity": err_parity},
+            "e2e": {"value": n / float(np.mean(e2e)), "unit": "tensors/s", "h2d_bytes_per_step": n * 36,
+                    "d2h_bytes_per_step": n * 48},
+            "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cpu, "clocks": clocks,
+            "kernels": {k: {"launches": v[0], "total_ms": v[1]} for k, v in prof.items()},
+        }), flush=True)
+
+
+def cpu_eigen_sample(n=1 << 20):
+    from oracle import oracle as O
+    from tiralib_gb300 import workloads as W
+    m9 = W.eigen_batch(n, seed=4)
+    th = os.cpu_count() or 1
+    O.eig3_threads(m9[:4096], th)
+    t0 = time.perf_counter()
+    O.eig3_threads(m9, th)
+    t = time.perf_counter() - t0
+    return n / t, th, (f"2^{int(np.log2(n))} C3-recipe tensors through eigen.h's CPU solve (evals3_symmetric + "
+                       f"evec3_symmetric, C port), OpenMP over tensors")
+
+
+def measured_peaks():
+    path = os.path.join(HERE, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(path))
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured (MEASURED_PEAKS.json hbm_gbs, copy)"}
+    except Exception:
+        return {"hbm_gbs": 6800.0, "source": "fallback 6.8 TB/s"}
+
+
+def run_c3_reference(args, rank):
+    if rank != 0:
+        return
+    vals = []
+    th, desc = 1, ""
+    for _ in range(args.warmup):
+        cpu_eigen_sample()
+    for _ in range(args.steps):
+        v, th, desc = cpu_eigen_sample()
+        vals.append(v)
+    value = float(np.mean(vals))
+    print(json.dumps({"impl": "reference", "metric": C3_METRIC, "value": value, "unit": "tensors/s",
+                      "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                      "ms_per_step": 1e3 * (1 << 20) / value, "higher_is_better": True, "scaling": "weak",
+                      "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                      "config": {"workload": "C3 eigen, bounded sample"},
+                      "cpu_baseline": {"value": value, "unit": "tensors/s", "cores": th, "kind": "port",
+                                       "sample": desc},
+                      "e2e": {"value": value, "unit": "tensors/s", "h2d_bytes_per_step": 0,
+                              "d2h_bytes_per_step": 0}}), flush=True)
+
+
+# ----------------------------------------------------------------------------- C1: 2D
+
+C1_METRIC = "2D tensor-vote pixels/s (structure tensor sigma 1 -> stick+plate vote sigma 3 -> 2x2 eigen)"
+
+
+def run_c1(args, rank, world, local_rank):
+    import torch
+    import tiralib_gb300 as tv
+    from tiralib_gb300 import workloads as W
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    size = args.size or 512
+    img_np = W.curve_image(size, seed=1 + rank)
+    img = torch.from_numpy(img_np).to(dev)
+    n = img_np.size
+    st = torch.empty((size, size, 4), device=dev)
+    voted = torch.empty((size, size, 4), device=dev)
+    ev = torch.empty((n, 2), device=dev)
+    th = torch.empty((n, 2), device=dev)
+    sigma, w, samples = 3.0, 19, 20
+    S = ctypes.c_void_p
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def step(src, st_, vo, e, t, stream):
+        d = (ctypes.c_uint * 2)()
+        tv.api.call("tvgb_structure_tensor2", tv.api._ptr(src), size, size, 1.0, 1, tv.api._ptr(st_), d, stream)
+        tv.api.call("tvgb_tensorvote", tv.api._ptr(vo), tv.api._ptr(st_), sigma, 0.0, 1, w, size, size, 1, 1,
+                    samples, 0, stream)
+        tv.api.call("tvgb_evals2_symmetric", tv.api._ptr(vo), n, tv.api._ptr(e), stream)
+        tv.api.call("tvgb_evecs2polar_symmetric", tv.api._ptr(vo), tv.api._ptr(e), n, tv.api._ptr(t), stream)
+
+    stream = S(torch.cuda.current_stream().cuda_stream)
+    for _ in range(args.warmup):
+        step(img, st, voted, ev, th, stream)
+    torch.cuda.synchronize()
+    lib = tv.lib()
+    buf = ctypes.create_string_buffer(1 << 14)
+    lib.tvgb_profile_enable(1)
+    lib.tvgb_profile_read(buf, len(buf))
+    l0 = tv.launch_count()
+    ts = []
+    with ClockSampler(gpu_index_for(local_rank)) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            step(img, st, voted, ev, th, stream)
+            e1.record()
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1))
+    launches = tv.launch_count() - l0
+    lib.tvgb_profile_read(buf, len(buf))
+    lib.tvgb_profile_enable(0)
+    prof = parse_profile(buf.value.decode())
+    t = float(np.sum(ts)) / 1e3
+    # end to end: host image in, host voted field + eigenpairs out
+    img_h = torch.from_numpy(img_np).pin_memory().numpy()
+    st_h = torch.empty((size, size, 4)).pin_memory().numpy()
+    vo_h = torch.empty((size, size, 4)).pin_memory().numpy()
+    ev_h = torch.empty((n, 2)).pin_memory().numpy()
+    th_h = torch.empty((n, 2)).pin_memory().numpy()
+    step(img_h, st_h, vo_h, ev_h, th_h, None)
+    e2e = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        step(img_h, st_h, vo_h, ev_h, th_h, None)
+        e2e.append(time.perf_counter() - t0)
+    # 2D pair: stick (q.d 3, q^2 1, 1-q^2 1, D 3, Rq 6, f 2, 3 accumulations 6, f Rq 2) 24 + plate 6 = 30 flops
+    pairs = 1
+    for d in (size, size):
+        pairs *= sum(min(d - 1, x + w // 2) - max(0, x - w // 2) + 1 for x in range(d))
+    nl, tot = prof.get("k_vote2_tk", (0, 0.0))
+    roof = None
+    if nl:
+        avg = tot / nl / 1e3
+        props = torch.cuda.get_device_properties(dev)
+        peak = props.multi_processor_count * FP32_LANES_PER_SM * 2 * 2070e6 / 1e12
+        ach = pairs * 30 / avg / 1e12
+        roof = {"bound": "fp32", "kernel": "k_vote2_tk", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
+                "frac": ach / peak, "flops_per_pair": 30, "avg_launch_ms": avg * 1e3,
+                "peak_source": "nominal FP32 at 2070 MHz", "traffic": profiled_traffic("k_vote2_tk")}
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        from oracle import oracle as O
+        crop = img_np[:192, :192]
+        t0 = time.perf_counter()
+        st_c = O.structure_tensor2(crop, 1.0, 1)
+        vo_c = O.tensorvote2(st_c, sigma, 0.0, 1, w, samples=samples)
+        e_c = O.evals2(vo_c)
+        O.evecs2polar(vo_c, e_c)
+        tc = time.perf_counter() - t0
+        cpu = {"value": crop.size / tc, "unit": "pixels/s", "cores": 1, "kind": "port",
+               "sample": "192x192 crop: the reference's CPU 2D path (tira::cpu::tensorvote's algorithm, single "
+                         "thread as shipped) incl. structure tensor and eigenpairs"}
+    if rank == 0:
+        print(json.dumps({
+            "metric": C1_METRIC, "value": world * args.steps * n / t, "unit": "pixels/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"C1: {size}^2 image of 32 random cubic Bezier curves (width 1.5) + N(0, 0.05); "
+                                   "np.gradient structure tensor, Gaussian sigma 1 (same size); TK stick + plate "
+                                   "vote sigma 3, w 19, samples 20; 2x2 eigenpairs", "pixels": n},
+            "e2e": {"value": n / float(np.mean(e2e)), "unit": "pixels/s", "h2d_bytes_per_step": img_np.nbytes,
+                    "d2h_bytes_per_step": st_h.nbytes + vo_h.nbytes + ev_h.nbytes + th_h.nbytes},
+            "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cpu, "clocks": clk.summary(),
+            "kernels": {k: {"launches": v[0], "total_ms": v[1]} for k, v in prof.items()},
+        }), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -367,12 +681,23 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--ref-block", type=int, default=12, help="edge of the CPU reference's receiver block")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--size", type=int, default=256, help="volume edge (256 = the benchmark workload; smaller "
-                                                          "sizes are for profiler captures)")
+    ap.add_argument("--config", choices=["c2", "c3", "c1"], default="c2",
+                    help="c2: 3D pipeline (the headline); c3: batched 3x3 eigen; c1: 2D pipeline")
+    ap.add_argument("--size", type=int, default=0, help="c2: volume edge (default 256); c3: log2 of the tensor "
+                                                        "count (default 27); c1: image edge (default 512). Smaller "
+                                                        "sizes are for profiler captures")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     rank, world, local_rank = dist_env()
+    if args.config == "c3":
+        return run_c3_reference(args, rank) if args.impl == "reference" else run_c3(args, rank, world, local_rank)
+    if args.config == "c1":
+        if args.impl == "reference":
+            return
+        return run_c1(args, rank, world, local_rank)
+    if not args.size:
+        args.size = 256
     if args.impl == "reference":
         run_reference(args, rank)
         return

@@ -57,6 +57,7 @@ _ORACLE_SIGS = {
     "or_evecs3spherical": (None, [_P, _P, _SZ, _P]),
     "or_evecs3cart": (None, [_P, _P, _SZ, _P]),
     "or_eig3_f64_batch": (None, [_P, _SZ, _P, _P]),
+    "or_eig3_batch_threads": (None, [_P, _SZ, _P, _P, _I]),
     "or_ksize3": (_U, [_F]),
     "or_ksize2": (_U, [_F]),
     "or_gaussian1d": (None, [_U, _F, _P]),
@@ -152,6 +153,16 @@ def evecs2polar(m4, ev2, use_ref=False):
     out = np.empty((m4.shape[0], 2), np.float32)
     (ref().ref_evecs2polar if use_ref else lib().or_evecs2polar)(_ptr(m4), _ptr(ev2), m4.shape[0], _ptr(out))
     return out
+
+
+def eig3_threads(m9, threads):
+    """eigen.h's FP32 solve (eigenvalues + cartesian eigenvectors) over a
+    batch, OpenMP over matrices."""
+    m9 = _f32(m9).reshape(-1, 9)
+    ev = np.empty((m9.shape[0], 3), np.float32)
+    vec = np.empty((m9.shape[0], 3, 3), np.float32)
+    lib().or_eig3_batch_threads(_ptr(m9), m9.shape[0], _ptr(ev), _ptr(vec), threads)
+    return ev, vec
 
 
 def eig3_f64(s6):

@@ -19,6 +19,7 @@ void or_spherical_to_cartesian(float theta, float phi, float* out3);
 void or_evals3(const float* m9, size_t n, float* evals3);
 void or_evecs3spherical(const float* m9, const float* evals3, size_t n, float* out6);
 void or_evecs3cart(const float* m9, const float* evals3, size_t n, float* out9);
+void or_eig3_batch_threads(const float* m9, size_t n, float* evals3, float* evecs9, int threads);
 void or_eig3_f64(const double* s6, double* evals3, double* evecs9);
 void or_eig3_f64_batch(const double* s6, size_t n, double* evals3, double* evecs9);
 /* filter / gradient / structure tensor (tira/functions/filter.h, tira/volume.h) */

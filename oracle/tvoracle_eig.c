@@ -14,6 +14,9 @@
 #include "tvoracle.h"
 #include <math.h>
 #include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 #define EIG_EPS 1e-6f          /* tira::constant::TIRA_EIGEN_EPSILON<float>, eigen.h:13 */
 #define PI_D 3.14159265358979323846
@@ -271,6 +274,23 @@ void or_evecs3cart(const float* m9, const float* evals3, size_t n, float* out9) 
         const float* m = m9 + 9 * i;
         or_evec3(m[0], m[1], m[4], m[2], m[5], m[8], evals3 + 3 * i, out9 + 9 * i, out9 + 9 * i + 3, out9 + 9 * i + 6);
     }
+}
+
+/* cpu::evals3_symmetric + evecs3 over a batch, spread over OpenMP threads
+ * (a harness loop for timing the reference's CPU eigensolver on all cores;
+ * the per-matrix arithmetic is or_eval3 / or_evec3 unchanged). */
+void or_eig3_batch_threads(const float* m9, size_t n, float* evals3, float* evecs9, int threads) {
+#ifdef _OPENMP
+    if (threads < 1) threads = 1;
+#pragma omp parallel for schedule(static) num_threads(threads)
+#endif
+    for (long long i = 0; i < (long long)n; ++i) {
+        const float* m = m9 + 9 * i;
+        or_eval3(m[0], m[1], m[4], m[2], m[5], m[8], &evals3[3 * i], &evals3[3 * i + 1], &evals3[3 * i + 2]);
+        or_evec3(m[0], m[1], m[4], m[2], m[5], m[8], evals3 + 3 * i, evecs9 + 9 * i, evecs9 + 9 * i + 3,
+                 evecs9 + 9 * i + 6);
+    }
+    (void)threads;
 }
 
 /* ---------------- FP64 precision oracle (no reference counterpart) ----------------
