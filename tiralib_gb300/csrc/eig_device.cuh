@@ -293,16 +293,18 @@ __device__ __forceinline__ void assemble(bool iso_high, T lw, const T* w, T lx, 
     if (ev[0] > ev[1]) { swapf_d(ev[0], ev[1]); for (int k = 0; k < 3; ++k) swapf_d(v0[k], v1[k]); }
 }
 
-// FP32 phase: returns true (and leaves ev / v* unset, w and iso_high set)
-// when the pair needs the FP64 phase.
-__device__ __forceinline__ bool eig3_precise_fp32(float a, float b, float c, float d, float e, float f, float* ev,
-                                                  float* v0, float* v1, float* v2, float* w, bool& iso_high) {
+// FP32 phase.  Returns 0 when done (ev / v* set); otherwise w and iso_high
+// are set and the return value selects the FP64 phase: 1 = the remaining
+// pair is closer than 1e-4 |lambda_max| (project onto the plane in FP64),
+// 2 = Smith's formula isolated no eigenvalue (a near-triple cluster: Jacobi).
+__device__ __forceinline__ int eig3_precise_fp32(float a, float b, float c, float d, float e, float f, float* ev,
+                                                 float* v0, float* v1, float* v2, float* w, bool& iso_high) {
     const float amax = fmaxf(fmaxf(fmaxf(fabsf(a), fabsf(b)), fmaxf(fabsf(c), fabsf(d))), fmaxf(fabsf(e), fabsf(f)));
     iso_high = true;
     if (amax == 0.0f || !(amax < INFINITY)) {
         ev[0] = ev[1] = ev[2] = amax == 0.0f ? 0.0f : NAN;
         v0[0] = 1; v0[1] = 0; v0[2] = 0; v1[0] = 0; v1[1] = 1; v1[2] = 0; v2[0] = 0; v2[1] = 0; v2[2] = 1;
-        return false;
+        return 0;
     }
     int ex;
     frexpf(amax, &ex);
@@ -318,36 +320,90 @@ __device__ __forceinline__ bool eig3_precise_fp32(float a, float b, float c, flo
     w[0] *= iw; w[1] *= iw; w[2] *= iw;
     float lx, ly, lw, rw, x[3], y[3];
     complement_solve<float>(A, w, lx, ly, x, y, lw, rw);
+    if (rw > 1e-10f) return 2;      // w's residual well above FP32 rounding
     const float lm = fmaxf(fmaxf(fabsf(lx), fabsf(ly)), fabsf(lw));
-    // FP32 suffices unless the pair is near-degenerate or Smith's formula could
-    // not isolate any eigenvalue (w's residual well above FP32 rounding)
-    if ((ly - lx) >= 1e-4f * lm && rw <= 1e-10f) {
-        assemble<float>(iso_high, lw, w, lx, ly, x, y, ev, v0, v1, v2, unsc);
-        return false;
-    }
-    return true;
+    if ((ly - lx) < 1e-4f * lm) return 1;
+    assemble<float>(iso_high, lw, w, lx, ly, x, y, ev, v0, v1, v2, unsc);
+    return 0;
 }
 
-// FP64 phase for a pair closer than 1e-4 |lambda_max|: the plane projection,
-// the 2x2 solve, the Rayleigh quotients and the frame in double precision.
+// FP64 phase.  code 1: the pair is resolved on the plane normal to w.  The
+// plane basis is exact: U = e_k x w copies two components of w (k = the
+// smallest |w_k|), V = w x U is formed in FP64, so w, U, V are orthogonal to
+// FP64 rounding and |V|^2 = |w|^2 |U|^2.  The 2x2 matrix H = [U V]^T A [U V]
+// is formed in FP64; with the Gram scaling folded in (H' = diag(1, 1/|w|)
+// H diag(1, 1/|w|) / |U|^2, |w|^2 = 1 + O(eps32) so 1/|w| and 1/|w|^2 are
+// two-term series) its difference and off-diagonal, which cancel for a close
+// pair, are exact to FP64 rounding.  The Jacobi angle needs only FP32
+// relative accuracy from those two numbers, the pair's eigenvalues come from
+// the rotated FP64 diagonal, and the frame is completed in FP32.
+// code 2: cyclic Jacobi on the whole matrix in FP64.
 __device__ __forceinline__ void eig3_precise_fp64(float a, float b, float c, float d, float e, float f, const float* w,
-                                                  bool iso_high, float* ev, float* v0, float* v1, float* v2) {
+                                                  bool iso_high, int code, float* ev, float* v0, float* v1, float* v2) {
     const float amax = fmaxf(fmaxf(fmaxf(fabsf(a), fabsf(b)), fmaxf(fabsf(c), fabsf(d))), fmaxf(fabsf(e), fabsf(f)));
     int ex;
     frexpf(amax, &ex);
     const float sc = ldexpf(1.0f, 1 - ex), unsc = ldexpf(1.0f, ex - 1);
-    const double Ad[6] = {double(a * sc), double(b * sc), double(d * sc), double(c * sc), double(e * sc), double(f * sc)};
-    double wd[3] = {w[0], w[1], w[2]};
-    const double nwd = 1.0 / sqrt(wd[0] * wd[0] + wd[1] * wd[1] + wd[2] * wd[2]);
-    wd[0] *= nwd; wd[1] *= nwd; wd[2] *= nwd;
-    double lxd, lyd, lwd, rwd, xd[3], yd[3];
-    complement_solve<double>(Ad, wd, lxd, lyd, xd, yd, lwd, rwd);
-    if (rwd <= 1e-10) {
-        assemble<double>(iso_high, lwd, wd, lxd, lyd, xd, yd, ev, v0, v1, v2, unsc);
+    if (code == 1) {
+        const float Af[6] = {a * sc, b * sc, d * sc, c * sc, e * sc, f * sc};   // xx xy xz yy yz zz
+        const double A[6] = {Af[0], Af[1], Af[2], Af[3], Af[4], Af[5]};
+        const float aw0 = fabsf(w[0]), aw1 = fabsf(w[1]), aw2 = fabsf(w[2]);
+        const int k = (aw0 <= aw1 && aw0 <= aw2) ? 0 : (aw1 <= aw2 ? 1 : 2);
+        float Uf[3];   // e_k x w, exact
+        if (k == 0) { Uf[0] = 0.0f; Uf[1] = -w[2]; Uf[2] = w[1]; }
+        else if (k == 1) { Uf[0] = w[2]; Uf[1] = 0.0f; Uf[2] = -w[0]; }
+        else { Uf[0] = -w[1]; Uf[1] = w[0]; Uf[2] = 0.0f; }
+        const double w0 = w[0], w1 = w[1], w2 = w[2], U0 = Uf[0], U1 = Uf[1], U2 = Uf[2];
+        const double V0 = w1 * U2 - w2 * U1, V1 = w2 * U0 - w0 * U2, V2 = w0 * U1 - w1 * U0;
+        const double nw = fma(w0, w0, fma(w1, w1, w2 * w2));
+        const double AU0 = fma(A[0], U0, fma(A[1], U1, A[2] * U2));
+        const double AU1 = fma(A[1], U0, fma(A[3], U1, A[4] * U2));
+        const double AU2 = fma(A[2], U0, fma(A[4], U1, A[5] * U2));
+        const double AV0 = fma(A[0], V0, fma(A[1], V1, A[2] * V2));
+        const double AV1 = fma(A[1], V0, fma(A[3], V1, A[4] * V2));
+        const double AV2 = fma(A[2], V0, fma(A[4], V1, A[5] * V2));
+        const double h00 = fma(U0, AU0, fma(U1, AU1, U2 * AU2));
+        const double h01 = fma(V0, AU0, fma(V1, AU1, V2 * AU2));
+        const double h11 = fma(V0, AV0, fma(V1, AV1, V2 * AV2));
+        const double dn = nw - 1.0;                                  // |dn| ~ 1e-7
+        const double inw = fma(dn, dn, 1.0 - dn);                    // 1 / |w|^2
+        const double isq = fma(0.375 * dn, dn, 1.0 - 0.5 * dn);      // 1 / |w|
+        const double g11 = h11 * inw, g01 = h01 * isq;               // |U|^2 H'
+        // Jacobi rotation of [[h00, g01], [g01, g11]] in FP32 from exact inputs
+        float cs = 1.0f, sn = 0.0f, tt = 0.0f;
+        if (g01 != 0.0) {
+            const float th = float(g11 - h00) / (2.0f * float(g01));
+            tt = (th >= 0.0f ? 1.0f : -1.0f) / (fabsf(th) + sqrtf(fmaf(th, th, 1.0f)));
+            cs = rsqrtf(fmaf(tt, tt, 1.0f));
+            sn = tt * cs;
+        }
+        const float nU = float(fma(U0, U0, fma(U1, U1, U2 * U2)));
+        const double lxd = fma(-double(tt), g01, h00), lyd = fma(double(tt), g01, g11);
+        float lx = float(lxd) / nU, ly = float(lyd) / nU;
+        const float iu = rsqrtf(nU), iv = rsqrtf(float(nw) * nU);
+        float x[3], y[3];
+        const float Vf[3] = {float(V0), float(V1), float(V2)};
+        for (int i = 0; i < 3; ++i) {
+            const float u = Uf[i] * iu, v = Vf[i] * iv;
+            x[i] = cs * u - sn * v;
+            y[i] = fmaf(sn, u, cs * v);
+        }
+        if (lxd > lyd) {   // ordered in FP64: the pair may round to one float
+            float tmp;
+            for (int i = 0; i < 3; ++i) { tmp = x[i]; x[i] = y[i]; y[i] = tmp; }
+            tmp = lx; lx = ly; ly = tmp;
+        }
+        // the isolated eigenvalue: FP32 Rayleigh quotient of w
+        const float Aw0 = fmaf(Af[0], w[0], fmaf(Af[1], w[1], Af[2] * w[2]));
+        const float Aw1 = fmaf(Af[1], w[0], fmaf(Af[3], w[1], Af[4] * w[2]));
+        const float Aw2 = fmaf(Af[2], w[0], fmaf(Af[4], w[1], Af[5] * w[2]));
+        const float lw = fmaf(w[0], Aw0, fmaf(w[1], Aw1, w[2] * Aw2)) / float(nw);
+        assemble<float>(iso_high, lw, w, lx, ly, x, y, ev, v0, v1, v2, unsc);
         return;
     }
+    const double A[6] = {double(a * sc), double(b * sc), double(d * sc), double(c * sc), double(e * sc), double(f * sc)};
     // no eigenvalue is isolated (a near-triple cluster): cyclic Jacobi in FP64
-    double M[3][3] = {{Ad[0], Ad[1], Ad[2]}, {Ad[1], Ad[3], Ad[4]}, {Ad[2], Ad[4], Ad[5]}};
+    double M[3][3] = {{A[0], A[1], A[2]}, {A[1], A[3], A[4]}, {A[2], A[4], A[5]}};
     double Q[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
     for (int sweep = 0; sweep < 8; ++sweep) {
         const double off = M[0][1] * M[0][1] + M[0][2] * M[0][2] + M[1][2] * M[1][2];
@@ -358,18 +414,18 @@ __device__ __forceinline__ void eig3_precise_fp64(float a, float b, float c, flo
             if (M[p][q] == 0.0) continue;
             const double th = (M[q][q] - M[p][p]) / (2.0 * M[p][q]);
             const double t = (th >= 0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
-            const double c = 1.0 / sqrt(t * t + 1.0), sn = t * c;
+            const double cc = 1.0 / sqrt(t * t + 1.0), ss = t * cc;
             for (int k = 0; k < 3; ++k) {
                 const double mkp = M[k][p], mkq = M[k][q];
-                M[k][p] = c * mkp - sn * mkq; M[k][q] = sn * mkp + c * mkq;
+                M[k][p] = cc * mkp - ss * mkq; M[k][q] = ss * mkp + cc * mkq;
             }
             for (int k = 0; k < 3; ++k) {
                 const double mpk = M[p][k], mqk = M[q][k];
-                M[p][k] = c * mpk - sn * mqk; M[q][k] = sn * mpk + c * mqk;
+                M[p][k] = cc * mpk - ss * mqk; M[q][k] = ss * mpk + cc * mqk;
             }
             for (int k = 0; k < 3; ++k) {
                 const double qkp = Q[k][p], qkq = Q[k][q];
-                Q[k][p] = c * qkp - sn * qkq; Q[k][q] = sn * qkp + c * qkq;
+                Q[k][p] = cc * qkp - ss * qkq; Q[k][q] = ss * qkp + cc * qkq;
             }
         }
     }
@@ -389,8 +445,9 @@ __device__ __forceinline__ bool eig3_precise_d(float a, float b, float c, float 
                                                float* v0, float* v1, float* v2) {
     float w[3];
     bool hi;
-    if (!eig3_precise_fp32(a, b, c, d, e, f, ev, v0, v1, v2, w, hi)) return false;
-    eig3_precise_fp64(a, b, c, d, e, f, w, hi, ev, v0, v1, v2);
+    const int code = eig3_precise_fp32(a, b, c, d, e, f, ev, v0, v1, v2, w, hi);
+    if (!code) return false;
+    eig3_precise_fp64(a, b, c, d, e, f, w, hi, code, ev, v0, v1, v2);
     return true;
 }
 

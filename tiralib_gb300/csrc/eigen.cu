@@ -85,10 +85,11 @@ __global__ void __launch_bounds__(EIG_BLOCK) k_eig3(const float* __restrict__ in
             if (PRECISE) {
                 float w[3];
                 bool hi;
-                if (eig3_precise_fp32(a, b, c, d, e, f, ev, v, v + 3, v + 6, w, hi)) {
-                    // queue for the FP64 phase; park w and the isolated side in s_vec
+                const int code = eig3_precise_fp32(a, b, c, d, e, f, ev, v, v + 3, v + 6, w, hi);
+                if (code) {
+                    // queue for the FP64 phase; park w, the isolated side and the code in s_vec
                     s_q[atomicAdd(&s_qn, 1)] = t;
-                    v[0] = w[0]; v[1] = w[1]; v[2] = w[2]; v[3] = hi ? 1.0f : 0.0f;
+                    v[0] = w[0]; v[1] = w[1]; v[2] = w[2]; v[3] = hi ? 1.0f : 0.0f; v[4] = float(code);
                 }
             } else {
                 if (EVALS_IN) { ev[0] = s_ev[t * 3]; ev[1] = s_ev[t * 3 + 1]; ev[2] = s_ev[t * 3 + 2]; }
@@ -111,8 +112,9 @@ __global__ void __launch_bounds__(EIG_BLOCK) k_eig3(const float* __restrict__ in
                 else { a = m[0]; b = m[1]; d = m[2]; c = m[3]; e = m[4]; f = m[5]; }
                 const float w[3] = {s_vec[u * 9], s_vec[u * 9 + 1], s_vec[u * 9 + 2]};
                 const bool hi = s_vec[u * 9 + 3] != 0.0f;
+                const int code = int(s_vec[u * 9 + 4]);
                 float ev[3], v[9];
-                eig3_precise_fp64(a, b, c, d, e, f, w, hi, ev, v, v + 3, v + 6);
+                eig3_precise_fp64(a, b, c, d, e, f, w, hi, code, ev, v, v + 3, v + 6);
                 s_ev[u * 3] = ev[0]; s_ev[u * 3 + 1] = ev[1]; s_ev[u * 3 + 2] = ev[2];
                 for (int k = 0; k < 9; ++k) s_vec[u * 9 + k] = v[k];
             }
