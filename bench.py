@@ -41,7 +41,14 @@ sys.path.insert(0, HERE)
 
 METRIC = "3D tensor-vote voxels/s (σ=4): surrogate vs plain, same GB300, ≤1e-3 rel err"
 
-C2 = dict(n=256, n_tubes=64, r_range=(1.0, 3.0), noise_sd=0.05, seed=2, sigma_st=1.5, sigma=4.0, w=25, samples=20)
+C2 = dict(name="C2", n=256, n_tubes=64, r_range=(1.0, 3.0), noise_sd=0.05, seed=2, n_sheets=0, sigma_st=1.5,
+          sigma=4.0, w=25, samples=20, ball=False)
+# the 384^3 field of the surrogate study, run here on the plain path
+C4 = dict(C2, name="C4", n=384, seed=4)
+# capacity: tubes and sheets, stick + plate + ball at sigma 6
+C5 = dict(name="C5", n=512, n_tubes=256, r_range=(1.0, 4.0), noise_sd=0.1, seed=5, n_sheets=32, sigma_st=2.0,
+          sigma=6.0, w=37, samples=20, ball=True)
+CONFIGS3 = {"c2": C2, "c4": C4, "c5": C5}
 
 # Algorithmic FP32 flops per in-bounds (receiver, voter) pair of the fast
 # kernel, FMA = 2, counted from the formulas in tiralib_gb300/csrc/vote3.cu:
@@ -49,6 +56,8 @@ C2 = dict(n=256, n_tubes=64, r_range=(1.0, 3.0), noise_sd=0.05, seed=2, sigma_st
 #   plate (closed form): n.o 2, 2vg 1, m 6, h 6, v^2 1, cA 2, sA 1, sB 1, identity 1,
 #                        sA*m 3, sB*h 3, 12 accumulations 24 = 51
 FLOPS_PER_PAIR = 28 + 51
+#   ball (closed form): identity 2, lb*w 1, w*o 3, 6 accumulations 12 = 18
+FLOPS_PER_PAIR_BALL = 18
 FP32_LANES_PER_SM = 128
 
 
@@ -165,12 +174,39 @@ def cpu_reference_sample(vol, cfg, block=16, seed=0, threads=None):
     return time.perf_counter() - t0, rec.size, threads
 
 
+def config3(args):
+    cfg = dict(CONFIGS3[args.config])
+    if args.size:
+        cfg["n"] = args.size
+    return cfg
+
+
+def make_volume(cfg, dev=None):
+    """The config's tube (and sheet) volume: on the host below 384^3, else
+    rasterised on `dev` (same geometry; device-generator noise)."""
+    from tiralib_gb300 import workloads as W
+    kw = dict(n_tubes=cfg["n_tubes"], r_range=cfg["r_range"], noise_sd=cfg["noise_sd"], seed=cfg["seed"],
+              n_sheets=cfg["n_sheets"])
+    if dev is not None and cfg["n"] >= 384:
+        return W.tube_volume_device(cfg["n"], dev, **kw)
+    return W.tube_volume(cfg["n"], **kw)
+
+
+def metric_for(cfg):
+    if cfg["name"] == "C2":
+        return METRIC
+    return (f"3D tensor-vote voxels/s ({cfg['name']}: sigma={cfg['sigma']:g}, "
+            f"stick+plate{'+ball' if cfg['ball'] else ''}, plain path)")
+
+
 def run_reference(args, rank):
     if rank != 0:
         return
-    from tiralib_gb300 import workloads as W
-    cfg = dict(C2, n=args.size)
-    vol = W.tube_volume(cfg["n"], cfg["n_tubes"], cfg["r_range"], noise_sd=cfg["noise_sd"], seed=cfg["seed"])
+    import torch
+    cfg = config3(args)
+    vol = make_volume(cfg, torch.device("cuda", 0) if torch.cuda.is_available() else None)
+    if not isinstance(vol, np.ndarray):
+        vol = vol.cpu().numpy()
     for i in range(args.warmup):
         cpu_reference_sample(vol, cfg, block=args.ref_block, seed=1000 + i)
     times, nrec, th = [], 0, 1
@@ -179,11 +215,12 @@ def run_reference(args, rank):
         times.append(t)
     total = float(np.sum(times))
     value = args.steps * nrec / total
-    sample = (f"{args.ref_block}^3 interior receivers (+{cfg['w'] // 2}-voxel window halo) of the 256^3 volume per "
-              f"step: structure tensor, stick + {cfg['samples']}-sample plate (tira::cpu::tensorvote3's algorithm), "
-              f"3x3 eigen of the voted tensors; OpenMP over receivers")
+    sample = (f"{args.ref_block}^3 interior receivers (+{cfg['w'] // 2}-voxel window halo) of the {cfg['n']}^3 "
+              f"volume per step: structure tensor, stick + {cfg['samples']}-sample plate (tira::cpu::tensorvote3's "
+              f"algorithm{'; the reference has no TK ball' if cfg['ball'] else ''}), 3x3 eigen of the voted tensors; "
+              f"OpenMP over receivers")
     line = {
-        "impl": "reference", "metric": METRIC, "value": value, "unit": "voxels/s", "n_gpus": args.gpus,
+        "impl": "reference", "metric": metric_for(cfg), "value": value, "unit": "voxels/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": config_dict(cfg),
@@ -195,11 +232,15 @@ def run_reference(args, rank):
 
 def config_dict(cfg):
     n = cfg["n"]
-    return {"workload": f"C2: {n}^3 tube volume -> structure tensor (sigma 1.5) -> TK stick+plate vote (sigma 4, "
-                        "w 25, samples 20) -> fused 3x3 eigendecomposition",
+    terms = "stick+plate+ball" if cfg["ball"] else "stick+plate"
+    sheets = f" + {cfg['n_sheets']} sheets" if cfg["n_sheets"] else ""
+    return {"workload": f"{cfg['name']}: {n}^3 tube volume{sheets} -> structure tensor (sigma {cfg['sigma_st']:g}) -> "
+                        f"TK {terms} vote (sigma {cfg['sigma']:g}, w {cfg['w']}, samples {cfg['samples']}) -> fused "
+                        "3x3 eigendecomposition",
             "volume": [cfg["n"]] * 3, "tubes": cfg["n_tubes"], "tube_radius": list(cfg["r_range"]),
-            "noise_sd": cfg["noise_sd"], "seed": cfg["seed"], "sigma_structure": cfg["sigma_st"],
-            "sigma_vote": cfg["sigma"], "window": cfg["w"], "samples": cfg["samples"], "power": 1,
+            "sheets": cfg["n_sheets"], "noise_sd": cfg["noise_sd"], "seed": cfg["seed"],
+            "sigma_structure": cfg["sigma_st"], "sigma_vote": cfg["sigma"], "window": cfg["w"],
+            "samples": cfg["samples"], "power": 1, "ball": cfg["ball"],
             "path": "plain (exact plate orientation integral, no surrogate)",
             "l2_flush": "256 MiB write between timed steps (outside the events)"}
 
@@ -213,9 +254,10 @@ def parse_profile(text):
     return out
 
 
-def profiled_traffic(kernel):
-    """DRAM bytes per launch from a committed ncu summary, if one exists."""
-    path = os.path.join(HERE, "profiles", f"{kernel}_c2.md")
+def profiled_traffic(kernel, workload="c2"):
+    """DRAM bytes per launch from the committed ncu summary of that kernel on
+    that workload (profiles/<kernel>_<workload>.md), if one exists."""
+    path = os.path.join(HERE, "profiles", f"{kernel}_{workload}.md")
     if not os.path.exists(path):
         return None
     for line in open(path):
@@ -239,8 +281,10 @@ def run_ours(args, rank, world, local_rank):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=dev)
-    cfg = dict(C2, n=args.size)
-    vol_np = W.tube_volume(cfg["n"], cfg["n_tubes"], cfg["r_range"], noise_sd=cfg["noise_sd"], seed=cfg["seed"])
+    cfg = config3(args)
+    vol = make_volume(cfg, dev)
+    vol_np = vol if isinstance(vol, np.ndarray) else vol.cpu().numpy()
+    del vol
     nvox = vol_np.size
     dims = vol_np.shape
     vol_h = torch.from_numpy(vol_np).pin_memory()
@@ -250,7 +294,7 @@ def run_ours(args, rank, world, local_rank):
     vec_d = torch.empty(dims + (3, 3), device=dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     kw = dict(sigma_st=cfg["sigma_st"], sigma1=cfg["sigma"], w=cfg["w"], samples=cfg["samples"], st_mode="same",
-              out_layout="planes", evecs="cartesian")
+              out_layout="planes", evecs="cartesian", ball=cfg["ball"])
 
     def step():
         tv.pipeline3(vol_d, outputs=(out_d, ev_d, vec_d), **kw)
@@ -262,6 +306,8 @@ def run_ours(args, rank, world, local_rank):
         dist.barrier()
     stream = torch.cuda.current_stream()
     lib = tv.lib()
+    torch.cuda.reset_peak_memory_stats(dev)
+    tv.memory_stats(reset_peak=True)
     lib.tvgb_profile_enable(1)
     buf = ctypes.create_string_buffer(1 << 14)
     lib.tvgb_profile_read(buf, len(buf))        # clear
@@ -280,6 +326,11 @@ def run_ours(args, rank, world, local_rank):
             times.append(e0.elapsed_time(e1))
         torch.cuda.synchronize()
     launches = tv.launch_count() - l0
+    free_b, total_b = torch.cuda.mem_get_info(dev)
+    memory = {"torch_tensors_peak_bytes": int(torch.cuda.max_memory_allocated(dev)),
+              "library_scratch_peak_bytes": tv.memory_stats()[1],
+              "device_used_bytes_after": int(total_b - free_b), "device_total_bytes": int(total_b)}
+    memory["peak_hbm_bytes"] = memory["torch_tensors_peak_bytes"] + memory["library_scratch_peak_bytes"]
     lib.tvgb_profile_read(buf, len(buf))
     lib.tvgb_profile_enable(0)
     prof = parse_profile(buf.value.decode())
@@ -329,13 +380,13 @@ def run_ours(args, rank, world, local_rank):
     roofline = None
     if nl:
         avg_s = tot_ms / nl / 1e3
-        flops = pairs_count(dims, cfg["w"] // 2) * FLOPS_PER_PAIR
+        flops = pairs_count(dims, cfg["w"] // 2) * (FLOPS_PER_PAIR + (FLOPS_PER_PAIR_BALL if cfg["ball"] else 0))
         achieved = flops / avg_s / 1e12
         roofline = {"bound": "fp32", "kernel": "k_vote3_fast", "achieved": achieved, "peak": peak,
                     "unit": "TFLOP/s", "frac": achieved / peak,
                     "peak_source": f"nominal FP32: {sms} SMs x {FP32_LANES_PER_SM} FMA lanes x 2 x {max_mhz:.0f} MHz "
                                    "(max SM clock; MEASURED_PEAKS.json has no FP32 figure)",
-                    "traffic": profiled_traffic("k_vote3_fast"),
+                    "traffic": profiled_traffic("k_vote3_fast", args.config),
                     "flops_per_launch": flops, "avg_launch_ms": avg_s * 1e3,
                     "share_of_step": (tot_ms / (np.sum(times))) if np.sum(times) else None}
 
@@ -344,15 +395,18 @@ def run_ours(args, rank, world, local_rank):
         t, nrec, th = cpu_reference_sample(vol_np, cfg, block=args.ref_block, seed=0)
         cpu = {"value": nrec / t, "unit": "voxels/s", "cores": th, "kind": "port",
                "sample": f"{args.ref_block}^3 interior receivers of the same volume (+ window halo), the reference's "
-                         f"CPU algorithm (stick + {cfg['samples']}-sample plate) in oracle/, OpenMP over receivers"}
+                         f"CPU algorithm (stick + {cfg['samples']}-sample plate"
+                         f"{'; no ball: the reference has no TK ball' if cfg['ball'] else ''}) in oracle/, OpenMP over "
+                         "receivers"}
     if rank == 0:
         line = {
-            "metric": METRIC, "value": value, "unit": "voxels/s", "n_gpus": world, "steps": args.steps,
+            "metric": metric_for(cfg), "value": value, "unit": "voxels/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config_dict(cfg),
             "e2e": {"value": e2e_value, "unit": "voxels/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
             "kernels": {k: {"launches": v[0], "total_ms": v[1]} for k, v in prof.items()},
+            "memory": memory,
         }
         print(json.dumps(line), flush=True)
     if dist:
@@ -495,7 +549,7 @@ def run_c3(args, rank, world, local_rank):
         ach = n * bytes_per / avg / 1e9
         roof = {"bound": "hbm", "kernel": "k_eig3 (precise)", "achieved": ach, "peak": peaks["hbm_gbs"],
                 "unit": "GB/s", "frac": ach / peaks["hbm_gbs"], "peak_source": peaks["source"],
-                "traffic": profiled_traffic("k_eig3"), "bytes_per_tensor": bytes_per, "avg_launch_ms": avg * 1e3}
+                "traffic": profiled_traffic("k_eig3", "c3"), "bytes_per_tensor": bytes_per, "avg_launch_ms": avg * 1e3}
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         v, th, desc = cpu_eigen_sample()
@@ -615,6 +669,11 @@ def run_c1(args, rank, world, local_rank):
             e1.synchronize()
             ts.append(e0.elapsed_time(e1))
     launches = tv.launch_count() - l0
+    free_b, total_b = torch.cuda.mem_get_info(dev)
+    memory = {"torch_tensors_peak_bytes": int(torch.cuda.max_memory_allocated(dev)),
+              "library_scratch_peak_bytes": tv.memory_stats()[1],
+              "device_used_bytes_after": int(total_b - free_b), "device_total_bytes": int(total_b)}
+    memory["peak_hbm_bytes"] = memory["torch_tensors_peak_bytes"] + memory["library_scratch_peak_bytes"]
     lib.tvgb_profile_read(buf, len(buf))
     lib.tvgb_profile_enable(0)
     prof = parse_profile(buf.value.decode())
@@ -644,7 +703,7 @@ def run_c1(args, rank, world, local_rank):
         ach = pairs * 30 / avg / 1e12
         roof = {"bound": "fp32", "kernel": "k_vote2_tk", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
                 "frac": ach / peak, "flops_per_pair": 30, "avg_launch_ms": avg * 1e3,
-                "peak_source": "nominal FP32 at 2070 MHz", "traffic": profiled_traffic("k_vote2_tk")}
+                "peak_source": "nominal FP32 at 2070 MHz", "traffic": profiled_traffic("k_vote2_tk", "c1")}
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         from oracle import oracle as O
@@ -670,7 +729,46 @@ def run_c1(args, rank, world, local_rank):
                     "d2h_bytes_per_step": st_h.nbytes + vo_h.nbytes + ev_h.nbytes + th_h.nbytes},
             "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cpu, "clocks": clk.summary(),
             "kernels": {k: {"launches": v[0], "total_ms": v[1]} for k, v in prof.items()},
+            "memory": memory,
         }), flush=True)
+
+
+def run_c1_reference(args, rank):
+    """The reference's CPU 2D path (oracle port of tira::cpu::tensorvote,
+    single thread as shipped) on the full C1 image, per step."""
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    from tiralib_gb300 import workloads as W
+    size = args.size or 512
+    img = W.curve_image(size, seed=1)
+    sigma, w, samples = 3.0, 19, 20
+
+    def step():
+        st = O.structure_tensor2(img, 1.0, 1)
+        vo = O.tensorvote2(st, sigma, 0.0, 1, w, samples=samples)
+        e = O.evals2(vo)
+        O.evecs2polar(vo, e)
+
+    for _ in range(args.warmup):
+        step()
+    ts = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        step()
+        ts.append(time.perf_counter() - t0)
+    value = args.steps * img.size / float(np.sum(ts))
+    print(json.dumps({
+        "impl": "reference", "metric": C1_METRIC, "value": value, "unit": "pixels/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(ts)),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"C1: {size}^2 curve image, TK stick + plate vote sigma 3, w 19, samples 20, 2x2 "
+                               "eigenpairs", "pixels": img.size},
+        "cpu_baseline": {"value": value, "unit": "pixels/s", "cores": 1, "kind": "port",
+                         "sample": f"the full {size}^2 image per step: structure tensor, tira::cpu::tensorvote's "
+                                   "algorithm, eigenpairs (single thread, as shipped)"},
+        "e2e": {"value": value, "unit": "pixels/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
 
 
 def main():
@@ -681,11 +779,12 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--ref-block", type=int, default=12, help="edge of the CPU reference's receiver block")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--config", choices=["c2", "c3", "c1"], default="c2",
-                    help="c2: 3D pipeline (the headline); c3: batched 3x3 eigen; c1: 2D pipeline")
-    ap.add_argument("--size", type=int, default=0, help="c2: volume edge (default 256); c3: log2 of the tensor "
-                                                        "count (default 27); c1: image edge (default 512). Smaller "
-                                                        "sizes are for profiler captures")
+    ap.add_argument("--config", choices=["c2", "c4", "c5", "c3", "c1"], default="c2",
+                    help="c2: 3D pipeline, 256^3 (the headline); c4: the same at 384^3; c5: 512^3 tubes + sheets, "
+                         "sigma 6, stick + plate + ball (capacity); c3: batched 3x3 eigen; c1: 2D pipeline")
+    ap.add_argument("--size", type=int, default=0, help="c2/c4/c5: volume edge (default 256/384/512); c3: log2 of "
+                                                        "the tensor count (default 27); c1: image edge (default "
+                                                        "512). Smaller sizes are for profiler captures")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
@@ -693,11 +792,7 @@ def main():
     if args.config == "c3":
         return run_c3_reference(args, rank) if args.impl == "reference" else run_c3(args, rank, world, local_rank)
     if args.config == "c1":
-        if args.impl == "reference":
-            return
-        return run_c1(args, rank, world, local_rank)
-    if not args.size:
-        args.size = 256
+        return run_c1_reference(args, rank) if args.impl == "reference" else run_c1(args, rank, world, local_rank)
     if args.impl == "reference":
         run_reference(args, rank)
         return

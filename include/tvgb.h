@@ -211,6 +211,13 @@ double tvgb_sticknorm3(float sigma1, float sigma2, unsigned power);
  * (for launch accounting in benchmarks). */
 unsigned long long tvgb_launch_count(void);
 
+/* Device bytes the library itself holds in stream-ordered temporaries (host
+ * staging of caller arrays, voter records) and their high-water mark since
+ * the last reset (no reference counterpart: for footprint reports).  Caller
+ * arrays are not counted.  reset_peak != 0 restarts the mark at the current
+ * value after reading it. */
+int tvgb_memory_stats(unsigned long long* scratch_bytes, unsigned long long* scratch_peak_bytes, int reset_peak);
+
 /* Opt-in per-kernel timing (no reference counterpart; the reference has no
  * timers): while enabled, every launch is bracketed by a CUDA event pair on
  * its stream.  tvgb_profile_read resolves the recorded launches (waiting on

@@ -35,6 +35,7 @@ SIGNATURES = {
     "tvgb_last_error": (ctypes.c_char_p, []),
     "tvgb_version": (_I, []),
     "tvgb_launch_count": (ctypes.c_ulonglong, []),
+    "tvgb_memory_stats": (_I, [_P, _P, ctypes.c_int]),
     "tvgb_evals3_symmetric": (_I, [_P, _SZ, _P, _P]),
     "tvgb_evecs3spherical_symmetric": (_I, [_P, _P, _SZ, _P, _P]),
     "tvgb_evals2_symmetric": (_I, [_P, _SZ, _P, _P]),

@@ -337,9 +337,17 @@ def launch_count():
     return int(_lib.lib().tvgb_launch_count())
 
 
+def memory_stats(reset_peak=False):
+    """(bytes, peak bytes) of device memory libtvgb holds in its own
+    temporaries (tvgb_memory_stats); caller arrays are not counted."""
+    cur, peak = ctypes.c_ulonglong(0), ctypes.c_ulonglong(0)
+    call("tvgb_memory_stats", ctypes.byref(cur), ctypes.byref(peak), int(bool(reset_peak)))
+    return int(cur.value), int(peak.value)
+
+
 __all__ = [
     "TvgbError", "NB2_DTYPE", "evals3_symmetric", "evecs3spherical_symmetric", "evals2_symmetric",
     "evecs2polar_symmetric", "eig3", "gaussian_filter3d", "gaussian_convolve2", "structure_tensor3",
     "structure_tensor2", "tensorvote3", "tensorvote", "tensorvote_prebuilt", "build_neighbors2d", "sticknorm3",
-    "make_params", "vote3", "pipeline3", "launch_count",
+    "make_params", "vote3", "pipeline3", "launch_count", "memory_stats",
 ]

@@ -217,59 +217,83 @@ __device__ __forceinline__ void st_zstep(float (&acc)[6][K], const float (&v)[6]
     for (int o = 0; o < 6; ++o) { done[o] = acc[o][sd]; acc[o][sd] = 0.0f; }
 }
 
-template <int K, int J = 0>
+// slot j of the z-window, resolved by one indexed branch
+template <int K>
 __device__ __forceinline__ void st_zdispatch(int j, float (&acc)[6][K], const float (&v)[6], const float (&gw)[K],
                                              float (&done)[6]) {
-    if constexpr (J < K) {
-        if (j == J) st_zstep<K, J>(acc, v, gw, done);
-        else st_zdispatch<K, J + 1>(j, acc, v, gw, done);
+#define TVGB_ZCASE(J) \
+    case J:           \
+        if constexpr (J < K) st_zstep<K, J>(acc, v, gw, done); \
+        break;
+    switch (j) {
+        TVGB_ZCASE(0) TVGB_ZCASE(1) TVGB_ZCASE(2) TVGB_ZCASE(3) TVGB_ZCASE(4) TVGB_ZCASE(5) TVGB_ZCASE(6)
+        TVGB_ZCASE(7) TVGB_ZCASE(8) TVGB_ZCASE(9) TVGB_ZCASE(10) TVGB_ZCASE(11) TVGB_ZCASE(12)
+        default: break;
     }
+#undef TVGB_ZCASE
+}
+
+// twice volume<T>::gradient's rule (central difference inside, one-sided at
+// the edges); the factor 4 on the products is taken out by the z weights
+__device__ __forceinline__ float grad2(float lo, float c, float hi, int p, int S) {
+    if (S < 2) return 0.0f;
+    if (p == 0) return 2.0f * (hi - c);
+    if (p == S - 1) return 2.0f * (c - lo);
+    return hi - lo;
 }
 
 template <int K>
 __global__ void __launch_bounds__(STX * STY, 2) k_st3(StArgs a) {
+    static_assert(K <= ST_MAXT, "fixed-tap kernel");
     constexpr int EX = STX + K - 1, EY = STY + K - 1;   // EX even: 64-bit row loads stay aligned
     constexpr int RX = EX + 2, RY = EY + 2;
     constexpr int NT = STX * STY;
     constexpr int NR = (RY * RX + NT - 1) / NT;          // raw elements per thread per plane
+    constexpr int PS = EY * EX;                          // product points per plane
+    constexpr int NP = (PS + NT - 1) / NT;               // product points per thread
     __shared__ __align__(16) float raw[3 * RY * RX];
-    __shared__ __align__(16) float sT[6 * EY * EX];
+    __shared__ __align__(16) float sT[6 * PS];
     __shared__ __align__(16) float sY[6 * STY * EX];
     const int tid = threadIdx.x;
-    float gw[K];
+    float gw[K], gz[K];
 #pragma unroll
-    for (int k = 0; k < K; ++k) gw[k] = a.g[k];
+    for (int k = 0; k < K; ++k) { gw[k] = a.g[k]; gz[k] = 0.25f * a.g[k]; }
 
     const int ox0 = blockIdx.x * STX, oy0 = blockIdx.y * STY;
     const int oz_lo = blockIdx.z * a.zchunk, oz_hi = min(a.o0 - 1, oz_lo + a.zchunk - 1);
     const int iz_lo = oz_lo - a.off, iz_hi = oz_hi + K - 1 - a.off;
     const int ix0 = ox0 - a.off, iy0 = oy0 - a.off;
     const size_t on = size_t(a.o0) * a.o1 * a.o2;
+    const size_t plane = size_t(a.s1) * a.s2;
+    // every product point and its x/y neighbours inside the volume: no edge rules in x, y
+    const bool inner = ix0 >= 1 && ix0 + EX <= a.s2 - 1 && iy0 >= 1 && iy0 + EY <= a.s1 - 1;
 
     // owned outputs: channels 3h..3h+2 at (x0 + {0,1}, y) of every plane
     const int h = tid >> 7, ty = (tid >> 4) & 7, px = (tid & 15) * 2;
     const int y = oy0 + ty, x0 = ox0 + px;
 
+    // raw elements of this thread: in-plane offset, or -1 outside the volume / region
+    int foff[NR];
+#pragma unroll
+    for (int r = 0; r < NR; ++r) {
+        const int e = tid + r * NT;
+        const int ry = e / RX, rx = e - ry * RX;
+        const int gxr = ix0 - 1 + rx, gyr = iy0 - 1 + ry;
+        foff[r] = (e < RY * RX && (unsigned)gxr < (unsigned)a.s2 && (unsigned)gyr < (unsigned)a.s1) ? gyr * a.s2 + gxr
+                                                                                                  : -1;
+    }
     float pre[NR];
     auto fetch = [&](int p) {
         const bool zin = p >= 0 && p < a.s0;
+        const float* src = a.vol + size_t(zin ? p : 0) * plane;
 #pragma unroll
-        for (int r = 0; r < NR; ++r) {
-            const int e = tid + r * NT;
-            const int ry = e / RX, rx = e - ry * RX;
-            const int gx = ix0 - 1 + rx, gy = iy0 - 1 + ry;
-            pre[r] = (e < RY * RX && zin && (unsigned)gx < (unsigned)a.s2 && (unsigned)gy < (unsigned)a.s1)
-                         ? __ldg(a.vol + (size_t(p) * a.s1 + gy) * a.s2 + gx)
-                         : 0.0f;
-        }
+        for (int r = 0; r < NR; ++r) pre[r] = (zin && foff[r] >= 0) ? __ldg(src + foff[r]) : 0.0f;
     };
     auto store = [&](int p) {
         float* dst = raw + (((p % 3) + 3) % 3) * RY * RX;
 #pragma unroll
-        for (int r = 0; r < NR; ++r) {
-            const int e = tid + r * NT;
-            if (e < RY * RX) dst[e] = pre[r];
-        }
+        for (int r = 0; r < NR; ++r)
+            if (tid + r * NT < RY * RX) dst[tid + r * NT] = pre[r];
     };
     fetch(iz_lo - 1); store(iz_lo - 1);
     fetch(iz_lo); store(iz_lo);
@@ -289,19 +313,38 @@ __global__ void __launch_bounds__(STX * STY, 2) k_st3(StArgs a) {
             const float* R0 = raw + ((((iz - 1) % 3) + 3) % 3) * RY * RX;
             const float* R1 = raw + (((iz % 3) + 3) % 3) * RY * RX;
             const float* R2 = raw + ((((iz + 1) % 3) + 3) % 3) * RY * RX;
-            constexpr int ps = EY * EX;
-            for (int e = tid; e < ps; e += NT) {
-                const int ry = e / EX, rx = e - ry * EX;
-                const int gxp = ix0 + rx, gyp = iy0 + ry;
-                float gx = 0.0f, gy = 0.0f, gz = 0.0f;
-                if ((unsigned)gxp < (unsigned)a.s2 && (unsigned)gyp < (unsigned)a.s1) {
-                    const int c = (ry + 1) * RX + rx + 1;
-                    gx = grad1(R1[c - 1], R1[c], R1[c + 1], gxp, a.s2);
-                    gy = grad1(R1[c - RX], R1[c], R1[c + RX], gyp, a.s1);
-                    gz = grad1(R0[c], R1[c], R2[c], iz, a.s0);
+            if (inner && iz >= 1 && iz <= a.s0 - 2) {
+#pragma unroll
+                for (int q = 0; q < NP; ++q) {
+                    const int e = tid + q * NT;
+                    if (e < PS) {
+                        const int ry = e / EX, rx = e - ry * EX;
+                        const int c = (ry + 1) * RX + rx + 1;
+                        const float gx = R1[c + 1] - R1[c - 1];
+                        const float gy = R1[c + RX] - R1[c - RX];
+                        const float gzv = R2[c] - R0[c];
+                        sT[e] = gx * gx; sT[PS + e] = gx * gy; sT[2 * PS + e] = gx * gzv;
+                        sT[3 * PS + e] = gy * gy; sT[4 * PS + e] = gy * gzv; sT[5 * PS + e] = gzv * gzv;
+                    }
                 }
-                sT[e] = gx * gx; sT[ps + e] = gx * gy; sT[2 * ps + e] = gx * gz;
-                sT[3 * ps + e] = gy * gy; sT[4 * ps + e] = gy * gz; sT[5 * ps + e] = gz * gz;
+            } else {
+#pragma unroll
+                for (int q = 0; q < NP; ++q) {
+                    const int e = tid + q * NT;
+                    if (e < PS) {
+                        const int ry = e / EX, rx = e - ry * EX;
+                        const int gxp = ix0 + rx, gyp = iy0 + ry;
+                        float gx = 0.0f, gy = 0.0f, gzv = 0.0f;
+                        if ((unsigned)gxp < (unsigned)a.s2 && (unsigned)gyp < (unsigned)a.s1) {
+                            const int c = (ry + 1) * RX + rx + 1;
+                            gx = grad2(R1[c - 1], R1[c], R1[c + 1], gxp, a.s2);
+                            gy = grad2(R1[c - RX], R1[c], R1[c + RX], gyp, a.s1);
+                            gzv = grad2(R0[c], R1[c], R2[c], iz, a.s0);
+                        }
+                        sT[e] = gx * gx; sT[PS + e] = gx * gy; sT[2 * PS + e] = gx * gzv;
+                        sT[3 * PS + e] = gy * gy; sT[4 * PS + e] = gy * gzv; sT[5 * PS + e] = gzv * gzv;
+                    }
+                }
             }
         }
         __syncthreads();   // products ready; raw plane iz - 1 no longer read
@@ -309,7 +352,7 @@ __global__ void __launch_bounds__(STX * STY, 2) k_st3(StArgs a) {
         if (zin) {
             for (int it = tid; it < 6 * EX; it += NT) {
                 const int c = it / EX, rx = it - c * EX;
-                const float* col = sT + c * EY * EX + rx;
+                const float* col = sT + c * PS + rx;
                 float cv[EY];
 #pragma unroll
                 for (int r = 0; r < EY; ++r) cv[r] = col[r * EX];
@@ -345,7 +388,7 @@ __global__ void __launch_bounds__(STX * STY, 2) k_st3(StArgs a) {
             for (int o = 0; o < 6; ++o) v[o] = 0.0f;
         }
         float done[6];
-        st_zdispatch<K>((iz - iz_lo) % K, acc, v, gw, done);
+        st_zdispatch<K>((iz - iz_lo) % K, acc, v, gz, done);
         // the slot just completed began at plane iz - K + 1: output oz
         const int oz = iz - (K - 1) + a.off;
         if (oz >= oz_lo && y < a.o1) {

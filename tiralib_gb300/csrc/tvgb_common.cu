@@ -66,6 +66,7 @@ int DevArray::in(const void* p, size_t nbytes, cudaStream_t s) {
     }
     TVGB_CUDA(cudaMallocAsync(&dev, nbytes, s));
     owned = true;
+    scratch_track((long long)nbytes);
     TVGB_CUDA(cudaMemcpyAsync(dev, p, nbytes, cudaMemcpyHostToDevice, s));
     return TVGB_OK;
 }
@@ -81,6 +82,7 @@ int DevArray::out(void* p, size_t nbytes, cudaStream_t s, bool zero) {
     } else {
         TVGB_CUDA(cudaMallocAsync(&dev, nbytes, s));
         owned = true;
+        scratch_track((long long)nbytes);
     }
     if (zero) TVGB_CUDA(cudaMemsetAsync(dev, 0, nbytes, s));
     return TVGB_OK;
@@ -96,7 +98,18 @@ int Scratch::alloc(size_t bytes, cudaStream_t s) {
     stream = s;
     if (bytes == 0) return TVGB_OK;
     TVGB_CUDA(cudaMallocAsync(&p, bytes, s));
+    this->bytes = bytes;
+    scratch_track((long long)bytes);
     return TVGB_OK;
+}
+
+static std::atomic<long long> g_scratch_cur{0}, g_scratch_peak{0};
+
+void scratch_track(long long delta) {
+    const long long now = g_scratch_cur.fetch_add(delta) + delta;
+    long long pk = g_scratch_peak.load();
+    while (now > pk && !g_scratch_peak.compare_exchange_weak(pk, now)) {
+    }
 }
 
 }  // namespace tvgb
@@ -106,6 +119,14 @@ extern "C" {
 const char* tvgb_last_error(void) { return tvgb::g_last_error; }
 int tvgb_version(void) { return 100; }
 unsigned long long tvgb_launch_count(void) { return tvgb::launch_counter().load(); }
+
+int tvgb_memory_stats(unsigned long long* scratch_bytes, unsigned long long* scratch_peak_bytes, int reset_peak) {
+    const long long cur = tvgb::g_scratch_cur.load();
+    if (scratch_bytes) *scratch_bytes = (unsigned long long)(cur > 0 ? cur : 0);
+    if (scratch_peak_bytes) *scratch_peak_bytes = (unsigned long long)tvgb::g_scratch_peak.load();
+    if (reset_peak) tvgb::g_scratch_peak.store(cur > 0 ? cur : 0);
+    return TVGB_OK;
+}
 
 int tvgb_profile_enable(int on) {
     tvgb::g_prof_on.store(on ? 1 : 0);

@@ -71,6 +71,10 @@ bool is_device_ptr(const void* p);
 // A device view of a caller array: the caller's pointer if it is device
 // memory, else a stream-ordered temporary (filled from the host for inputs,
 // copied back by finish() for outputs).
+// Device bytes held by the library's own temporaries (stream-ordered
+// allocations, counted when enqueued / released), and their high-water mark.
+void scratch_track(long long delta);
+
 struct DevArray {
     void* user = nullptr;
     void* dev = nullptr;
@@ -83,7 +87,10 @@ struct DevArray {
     DevArray(const DevArray&) = delete;
     DevArray& operator=(const DevArray&) = delete;
     ~DevArray() {
-        if (owned && dev) cudaFreeAsync(dev, stream);
+        if (owned && dev) {
+            cudaFreeAsync(dev, stream);
+            scratch_track(-(long long)bytes);
+        }
     }
     template <class T> T* get() const { return static_cast<T*>(dev); }
     // input: copy host data in
@@ -97,12 +104,16 @@ struct DevArray {
 // Plain stream-ordered scratch buffer.
 struct Scratch {
     void* p = nullptr;
+    size_t bytes = 0;
     cudaStream_t stream = nullptr;
     Scratch() = default;
     Scratch(const Scratch&) = delete;
     Scratch& operator=(const Scratch&) = delete;
     ~Scratch() {
-        if (p) cudaFreeAsync(p, stream);
+        if (p) {
+            cudaFreeAsync(p, stream);
+            scratch_track(-(long long)bytes);
+        }
     }
     int alloc(size_t bytes, cudaStream_t s);
     template <class T> T* get() const { return static_cast<T*>(p); }

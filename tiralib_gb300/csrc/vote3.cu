@@ -154,6 +154,13 @@ __device__ __forceinline__ void kahan_add(float& sum, float& comp, float x) {
 #ifndef TVGB_FAST_MINB
 #define TVGB_FAST_MINB 2       // resident CTAs per SM the register budget is sized for
 #endif
+#ifndef TVGB_FOLD_PLANE
+#define TVGB_FOLD_PLANE 1      // 1: FP32 partials span a whole voter plane before the Kahan fold
+#endif
+#ifndef TVGB_DUNROLL
+#define TVGB_DUNROLL 2         // unroll factor of the +-ox loop
+#endif
+constexpr int kDUnroll = TVGB_DUNROLL;
 
 // one (receiver, voter) pair: stick + closed-form plate (+ ball) into P[0..6]
 template <bool STICK, bool PLATE, bool BALL>
@@ -214,16 +221,38 @@ __device__ __forceinline__ void vote_pair(const float4& A, const float4& B, floa
 // one row of voters (fixed vz, oy) against receivers j in [JLO, JHI].  The
 // weights depend on ox^2 only, so the voters at +ox and -ox are taken together
 // and share each table load.  rA / rB / rC point at this thread's ox = 0 voter.
+template <int R>
+__device__ __forceinline__ void fold_partials(float (&P)[R][7], float (&tot)[R][6], float (&cmp)[R][6], int jlo,
+                                              int jhi) {
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+        if (j < jlo || j > jhi) continue;
+        kahan_add(tot[j][0], cmp[j][0], P[j][0] + P[j][6]);
+        kahan_add(tot[j][1], cmp[j][1], P[j][1]);
+        kahan_add(tot[j][2], cmp[j][2], P[j][2]);
+        kahan_add(tot[j][3], cmp[j][3], P[j][3] + P[j][6]);
+        kahan_add(tot[j][4], cmp[j][4], P[j][4]);
+        kahan_add(tot[j][5], cmp[j][5], P[j][5] + P[j][6]);
+#pragma unroll
+        for (int k = 0; k < 7; ++k) P[j][k] = 0.0f;
+    }
+}
+
 template <int R, int JLO, int JHI, bool STICK, bool PLATE, bool BALL>
 __device__ __forceinline__ void vote_row(const float4* __restrict__ rA, const float4* __restrict__ rB,
                                          const float* __restrict__ rC, const float4* __restrict__ tbl,
                                          const int (&zoff)[R], const float (&ozf)[R], float oyf, int L2y, int hw,
-                                         float (&tot)[R][6], float (&cmp)[R][6]) {
+                                         float (&tot)[R][6], float (&cmp)[R][6], float (&Pp)[R][7]) {
+#if TVGB_FOLD_PLANE
+    float (&P)[R][7] = Pp;
+#else
+    (void)Pp;
     float P[R][7];
 #pragma unroll
     for (int j = 0; j < R; ++j)
 #pragma unroll
         for (int k = 0; k < 7; ++k) P[j][k] = 0.0f;
+#endif
     const float4 Z4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     {   // ox = 0
         const float4 A = STICK ? rA[0] : Z4, B = PLATE ? rB[0] : Z4;
@@ -240,7 +269,7 @@ __device__ __forceinline__ void vote_row(const float4* __restrict__ rA, const fl
     float oxf = 1.0f;
     int off = 2 * (1 + L2y);
     int step = 6;                        // 2 * (2 ox + 1) for ox = 1
-#pragma unroll 1
+#pragma unroll kDUnroll
     for (int d = 1; d <= hw; ++d) {
         const float4 Ap = STICK ? rA[d] : Z4, Am = STICK ? rA[-d] : Z4;
         const float4 Bp = PLATE ? rB[d] : Z4, Bm = PLATE ? rB[-d] : Z4;
@@ -258,35 +287,31 @@ __device__ __forceinline__ void vote_row(const float4* __restrict__ rA, const fl
         step += 4;
         oxf += 1.0f;
     }
+#if !TVGB_FOLD_PLANE
     // fold the row partials into the per-voxel Kahan sums
-#pragma unroll
-    for (int j = JLO; j <= JHI; ++j) {
-        kahan_add(tot[j][0], cmp[j][0], P[j][0] + P[j][6]);
-        kahan_add(tot[j][1], cmp[j][1], P[j][1]);
-        kahan_add(tot[j][2], cmp[j][2], P[j][2]);
-        kahan_add(tot[j][3], cmp[j][3], P[j][3] + P[j][6]);
-        kahan_add(tot[j][4], cmp[j][4], P[j][4]);
-        kahan_add(tot[j][5], cmp[j][5], P[j][5] + P[j][6]);
-    }
+    fold_partials<R>(P, tot, cmp, JLO, JHI);
+#endif
 }
 
 template <int R, int JLO, int JHI, bool S, bool PL, bool BA>
 __device__ __forceinline__ void row_if(int jlo, int jhi, const float4* rA, const float4* rB, const float* rC,
                                        const float4* tbl, const int (&zoff)[R], const float (&ozf)[R], float oyf,
-                                       int L2y, int hw, float (&tot)[R][6], float (&cmp)[R][6]) {
-    if (jlo == JLO && jhi == JHI) vote_row<R, JLO, JHI, S, PL, BA>(rA, rB, rC, tbl, zoff, ozf, oyf, L2y, hw, tot, cmp);
+                                       int L2y, int hw, float (&tot)[R][6], float (&cmp)[R][6], float (&P)[R][7]) {
+    if (jlo == JLO && jhi == JHI)
+        vote_row<R, JLO, JHI, S, PL, BA>(rA, rB, rC, tbl, zoff, ozf, oyf, L2y, hw, tot, cmp, P);
 }
 
 // every (jlo, jhi) with 0 <= jlo <= jhi < R
 template <int R, int JLO, int JHI, bool S, bool PL, bool BA>
 __device__ __forceinline__ void row_dispatch(int jlo, int jhi, const float4* rA, const float4* rB, const float* rC,
                                              const float4* tbl, const int (&zoff)[R], const float (&ozf)[R],
-                                             float oyf, int L2y, int hw, float (&tot)[R][6], float (&cmp)[R][6]) {
-    row_if<R, JLO, JHI, S, PL, BA>(jlo, jhi, rA, rB, rC, tbl, zoff, ozf, oyf, L2y, hw, tot, cmp);
+                                             float oyf, int L2y, int hw, float (&tot)[R][6], float (&cmp)[R][6],
+                                             float (&P)[R][7]) {
+    row_if<R, JLO, JHI, S, PL, BA>(jlo, jhi, rA, rB, rC, tbl, zoff, ozf, oyf, L2y, hw, tot, cmp, P);
     if constexpr (JHI + 1 < R)
-        row_dispatch<R, JLO, JHI + 1, S, PL, BA>(jlo, jhi, rA, rB, rC, tbl, zoff, ozf, oyf, L2y, hw, tot, cmp);
+        row_dispatch<R, JLO, JHI + 1, S, PL, BA>(jlo, jhi, rA, rB, rC, tbl, zoff, ozf, oyf, L2y, hw, tot, cmp, P);
     else if constexpr (JLO + 1 < R)
-        row_dispatch<R, JLO + 1, JLO + 1, S, PL, BA>(jlo, jhi, rA, rB, rC, tbl, zoff, ozf, oyf, L2y, hw, tot, cmp);
+        row_dispatch<R, JLO + 1, JLO + 1, S, PL, BA>(jlo, jhi, rA, rB, rC, tbl, zoff, ozf, oyf, L2y, hw, tot, cmp, P);
 }
 
 __device__ __forceinline__ void write_receiver(const FastArgs& a, size_t idx, size_t n, const float* m6) {
@@ -363,11 +388,14 @@ __global__ void __launch_bounds__(VX * VY, TVGB_FAST_MINB) k_vote3_fast(FastArgs
         const int jlo = max(0, dzp - hw), jhi = min(R - 1, dzp + hw);
         int zoff[R];
         float ozf[R];
+        float P[R][7];   // plane partials (TVGB_FOLD_PLANE); otherwise unused
 #pragma unroll
         for (int j = 0; j < R; ++j) {
             const int oz = dzp - j;
             zoff[j] = 2 * oz * oz;
             ozf[j] = float(oz);
+#pragma unroll
+            for (int k = 0; k < 7; ++k) P[j][k] = 0.0f;
         }
         for (int oy0 = -hw; oy0 <= hw; oy0 += a.rows) {
             const int oy1 = min(hw, oy0 + a.rows - 1);
@@ -392,9 +420,12 @@ __global__ void __launch_bounds__(VX * VY, TVGB_FAST_MINB) k_vote3_fast(FastArgs
                 const int rr = threadIdx.y + (oy - oy0);
                 const int base = rr * SW + threadIdx.x + hw;   // column of ox = 0
                 row_dispatch<R, 0, 0, STICK, PLATE, BALL>(jlo, jhi, sA + base, sB + base, sC + base, tbl, zoff, ozf,
-                                                          float(oy), oy * oy, hw, tot, cmp);
+                                                          float(oy), oy * oy, hw, tot, cmp, P);
             }
         }
+#if TVGB_FOLD_PLANE
+        fold_partials<R>(P, tot, cmp, jlo, jhi);
+#endif
     }
 
     const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
