@@ -204,6 +204,90 @@ int tvgb_pipeline3(const float* volume, unsigned s0, unsigned s1, unsigned s2, f
                    const tvgb_vote3_params* p, float* out, int out_layout, float* evals3, float* evecs,
                    int evec_format, unsigned* out_dims, void* stream);
 
+/* ---- Consumers of a voted 2D field (tiralib's Python layer,
+ * python/tira/tensors_lib/reconstruct.py and metrics.py, has no C or CUDA
+ * counterpart; these replace its NumPy / SciPy code for this path).  Fields
+ * are n pixels of [a, b, b, c] float32 (the 2D vote's layout); host or
+ * device pointers. */
+
+/* Replaces reconstruct.py:14 stick_saliency: |lambda|max - |lambda|min per
+ * pixel into saliency (n floats). */
+int tvgb_stick_saliency2(const float* field, size_t n, float* saliency, void* stream);
+
+/* Replaces reconstruct.py:34 _otsu_threshold: Otsu's threshold of n
+ * non-negative values (256-bin histogram over [0, max], NumPy's bin rules),
+ * written to *threshold (host). */
+int tvgb_otsu_threshold(const float* values, size_t n, double* threshold, void* stream);
+
+/* Replaces reconstruct.py:66 saliency_threshold on an s0 x s1 field: mask =
+ * saliency > threshold (Otsu's when use_otsu != 0); with fill != 0 the mask
+ * is closed with a (2 close_radius + 1)^2 square (border value 0) and its
+ * holes (background not 4-connected to the border) are filled, as
+ * scipy.ndimage.binary_closing + binary_fill_holes.  mask: s0 * s1 bytes
+ * (0 / 1).  threshold_used (host, may be NULL) receives the threshold. */
+int tvgb_saliency_threshold2(const float* field, unsigned s0, unsigned s1, int fill, int use_otsu, double threshold,
+                             int close_radius, unsigned char* mask, double* threshold_used, void* stream);
+
+/* Replaces metrics.py:37 simf: mean over pixels of ||A - alpha B||_F with
+ * alpha = <A,B> / <B,B> (0 when <B,B> < 1e-8), written to *simf (host). */
+int tvgb_simf2(const float* A, const float* B, size_t n, double* simf, void* stream);
+
+/* The objective evaluations of optimize.py:256 optimize_tk as one call: K
+ * parameter sets params[3k..3k+2] = (sigma1, sigma2, power) (power rounded
+ * down, >= 1) voted on t_in (TK stick + plate with `samples` plate samples
+ * when plate != 0; window 2 int(3 max(sigma1, sigma2)) + 1 as
+ * optimize.py:_w_from_sigma), each scored by simf against G into simf[k]
+ * (host).  The input is solved once for all K sets.  t_out, if not NULL,
+ * receives the K voted fields (K * shape0 * shape1 * 4 floats). */
+int tvgb_tensorvote_sweep(const float* t_in, const float* G, unsigned shape0, unsigned shape1, const double* params,
+                          int K, unsigned samples, int plate, double* simf, float* t_out, void* stream);
+
+/* ---- Learned plate / ball vote (no reference counterpart: the north-star
+ * surrogate of the reference's plate3_numerical_device, tensorvote.h:2457).
+ * The network is an MLP 7 -> 64 -> 64 -> 64 -> 6 (GELU; BF16 weights and
+ * activations on the tensor cores, FP32 accumulation) from
+ * (offset direction o / |o|, plate normal n, flag: 1 plate / 0 ball) to the
+ * vote's angular part (xx, xy, xz, yy, yz, zz) for sigma2 = 0, power 1,
+ * o != 0; the Gaussian exp(-|o|^2 / sigma^2) is applied analytically.  Parameters: a
+ * float32 vector of tvgb_surrogate_param_count() values, layout
+ * W1[64][8] b1[64] W2[64][64] b2[64] W3[64][64] b3[64] W4[8][64] b4[8]
+ * (W[out][in]; W1[.][7], W4[6..7][.], b4[6..7] zero).  Arrays are host or
+ * device pointers; X and T hold 8 floats per sample (inputs padded with a
+ * zero, targets with two). */
+int tvgb_surrogate_param_count(void);
+
+/* n training samples from the plain orientation integral (64 orientations;
+ * offset directions and normals uniform on the sphere, plate or ball with
+ * probability 1/2; counter-based random stream `seed`). */
+int tvgb_surrogate_samples(size_t n, unsigned long long seed, float* X, float* T, void* stream);
+
+/* One quantisation-aware forward + backward pass over batch samples (batch a
+ * multiple of 32): grad (param_count floats) = d loss / d params, *loss
+ * (host) = sum over samples and the 6 outputs of (y - t)^2 / batch. */
+int tvgb_surrogate_grad(const float* params, const float* X, const float* T, int batch, float* grad, float* loss,
+                        void* stream);
+
+/* `steps` Adam steps (batch samples each, cycling through the n samples;
+ * learning rate lr with cosine decay to lr / 100); params updated in place;
+ * loss_history (steps floats, may be NULL) gets each step's loss. */
+int tvgb_surrogate_train(float* params, const float* X, const float* T, size_t n, int batch, int steps, float lr,
+                         float* loss_history, void* stream);
+
+/* The network on the tensor cores: Y (n x 8 floats, 6 used) from X. */
+int tvgb_surrogate_eval(const float* params, const float* X, size_t n, float* Y, void* stream);
+
+/* tvgb_vote3 (TK, power 1, sigma2 = 0) with the plate (and ball) vote by
+ * plate_mode: 0 the network (judged per CTA of 32 x 4 receivers: if any of
+ * its first 32 receivers' plate differs from the exact plate by more than
+ * tol x its voted tensor's norm, the CTA's plate is voted exactly), 1 the
+ * exact closed form, 2 the plain 64-orientation integral.  The stick vote
+ * is exact in every mode.  stats (2 values, host, may be NULL): CTAs, and
+ * CTAs recomputed exactly. */
+int tvgb_vote3_surrogate(const float* in, int in_layout, unsigned s0, unsigned s1, unsigned s2,
+                         const tvgb_vote3_params* params, const float* net_params, int plate_mode, float tol,
+                         float* out, int out_layout, float* evals3, float* evecs, int evec_format,
+                         unsigned long long* stats, void* stream);
+
 /* Sticknorm of the 3D stick vote (tira::sticknorm3, tensorvote.h:1163), host. */
 double tvgb_sticknorm3(float sigma1, float sigma2, unsigned power);
 

@@ -51,6 +51,9 @@ class _Lib:
 
 
 _ORACLE_SIGS = {
+    "or_mlp_param_count": (_I, []),
+    "or_mlp_loss_grad": (_D, [_P, _P, _P, _I, _I, _P, _P]),
+    "or_surrogate_target": (None, [_P, _P, _I, _P]),
     "or_evals2": (None, [_P, _SZ, _P]),
     "or_evecs2polar": (None, [_P, _P, _SZ, _P]),
     "or_evals3": (None, [_P, _SZ, _P]),
@@ -314,3 +317,84 @@ def tensorvote2_prebuilt(in4, nb, sigma1, sigma2, power, w, stick=True, plate=Tr
     lib().or_tensorvote2_prebuilt(_ptr(out), _ptr(in4), _ptr(nb), nb.size, sigma1, sigma2, power, w, s0, s1,
                                   int(stick), int(plate), samples)
     return out
+
+
+# ---------------------------------------------------------------- consumers of a voted 2D field
+# NumPy / SciPy restatements of python/tira/tensors_lib/reconstruct.py and
+# metrics.py (the reference is itself NumPy; these are the checker's copy of
+# its rules, pinned against tests/golden/reconstruct_reference.npz).
+
+def stick_saliency(T):
+    """reconstruct.py:14: |lambda|max - |lambda|min per pixel of (H, W, 2, 2)."""
+    mags = np.sort(np.abs(np.linalg.eigvalsh(T)), axis=-1)
+    return mags[..., 1] - mags[..., 0]
+
+
+def otsu_threshold(values):
+    """reconstruct.py:34: Otsu on a 256-bin histogram over [0, max]."""
+    vmax = float(values.max())
+    if vmax <= 0:
+        return 0.0
+    hist, edges = np.histogram(values, bins=256, range=(0.0, vmax))
+    hist = hist.astype(np.float64)
+    if hist.sum() == 0:
+        return 0.0
+    centers = (edges[:-1] + edges[1:]) / 2.0
+    w0 = np.cumsum(hist)
+    w1 = hist.sum() - w0
+    cum = np.cumsum(hist * centers)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        mu0 = np.where(w0 > 0, cum / w0, 0.0)
+        mu1 = np.where(w1 > 0, (cum[-1] - cum) / w1, 0.0)
+    return float(centers[np.argmax(w0 * w1 * (mu0 - mu1) ** 2)])
+
+
+def saliency_threshold(T, fill=False, threshold="otsu", close_radius=0):
+    """reconstruct.py:66: saliency > threshold, optionally closed and hole-filled."""
+    from scipy.ndimage import binary_closing, binary_fill_holes
+    s = stick_saliency(T)
+    thr = otsu_threshold(s.ravel()) if threshold == "otsu" else float(threshold)
+    b = s > thr
+    if not fill:
+        return b
+    if close_radius > 0:
+        b = binary_closing(b, structure=np.ones((2 * close_radius + 1,) * 2, bool))
+    return binary_fill_holes(b)
+
+
+def simf(A, B):
+    """metrics.py:37: mean over pixels of ||A - alpha B||_F, alpha = <A,B>/<B,B>."""
+    A = np.asarray(A, np.float64)
+    B = np.asarray(B, np.float64)
+    den = np.sum(B * B)
+    alpha = 0.0 if den < 1e-8 else np.sum(A * B) / den
+    return float(np.mean(np.linalg.norm(A - alpha * B, axis=(-2, -1))))
+
+
+# ---------------------------------------------------------------- plate / ball surrogate (tvoracle_mlp.c)
+
+def mlp_param_count():
+    return int(lib().or_mlp_param_count())
+
+
+def mlp_loss_grad(params, X, T, quant=True):
+    """FP64 loss and gradient of the surrogate MLP over a batch: X (B, 8)
+    inputs, T (B, 8) targets (first 6 used).  Returns (loss, grad, Y)."""
+    P = np.ascontiguousarray(params, np.float64)
+    X = np.ascontiguousarray(X, np.float64).reshape(-1, 8)
+    T = np.ascontiguousarray(T, np.float64).reshape(-1, 8)
+    g = np.zeros(mlp_param_count())
+    Y = np.zeros_like(T)
+    loss = lib().or_mlp_loss_grad(_ptr(P), _ptr(X), _ptr(T), X.shape[0], int(quant), _ptr(g), _ptr(Y))
+    return float(loss), g, Y
+
+
+def surrogate_target(direction, normal, plate):
+    """The plain orientation integral (64 orientations; sigma2 = 0, power 1,
+    Gaussian factored out) for one offset direction and plate normal:
+    (xx, xy, xz, yy, yz, zz)."""
+    d = np.ascontiguousarray(direction, np.float64)
+    nn = np.ascontiguousarray(normal, np.float64)
+    F = np.zeros(6)
+    lib().or_surrogate_target(_ptr(d), _ptr(nn), int(plate), _ptr(F))
+    return F

@@ -45,6 +45,10 @@ void or_tensorvote2(float* out4, const float* in4, float s1, float s2, int power
                     int stick, int plate, unsigned samples, int is_atv);
 void or_tensorvote2_prebuilt(float* out4, const float* in4, const void* nb, int nbc, float s1, float s2, int power,
                              unsigned w, unsigned S0, unsigned S1, int stick, int plate, unsigned samples);
+/* plate / ball vote surrogate: FP64 MLP and its training target */
+int or_mlp_param_count(void);
+double or_mlp_loss_grad(const double* P, const double* X, const double* T, int B, int quant, double* grad, double* Y);
+void or_surrogate_target(const double* dir, const double* n, int plate, double* F);
 #ifdef __cplusplus
 }
 #endif

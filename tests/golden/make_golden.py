@@ -4,12 +4,15 @@ Run in a checkout where the tiralib reference tree is available:
 
     python tests/golden/make_golden.py <path to the tiralib checkout>
 
-Two reference sources are used, and nothing else:
+Three reference sources are used, and nothing else:
   * tiralib's own C++ CPU functions, compiled unmodified by oracle/build_ref.sh
     (glm / Boost replaced by the stand-ins in oracle/shim) -> oracle/_ref;
   * tiralib's NumPy 2D implementation python/tira/tensors.py (tk_vote2 at
     tensors.py:265, atv_vote2 at tensors.py:164), imported with its unused
-    plotting / skeleton dependencies stubbed out.
+    plotting / skeleton dependencies stubbed out;
+  * tiralib's field consumers python/tira/tensors_lib/reconstruct.py
+    (stick_saliency, _otsu_threshold, saliency_threshold) and metrics.py
+    (simf), imported as they are (NumPy / SciPy only).
 The field generators follow the reference tests' recipes
 (python/tira/tests/test_cpu_gpu.py:41-75, test_cuda_vs_python.py:48-91,
 test_analytical_vs_numerical.py:19-36) at smaller sizes so the fixtures
@@ -27,6 +30,13 @@ REPO = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, REPO)
 
 from oracle import oracle as O  # noqa: E402
+
+
+def load_reference_module(ref_root, rel, name):
+    spec = importlib.util.spec_from_file_location(name, os.path.join(ref_root, rel))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
 
 
 def load_reference_tensors(ref_root):
@@ -176,6 +186,47 @@ def main(ref_root):
     fx["img"] = img
     fx["conv2_1"] = O.gaussian_convolve2(img, 1.0, use_ref=True)
     np.savez_compressed(os.path.join(HERE, "filter_cpp_reference.npz"), **fx)
+
+    # --- consumers of a voted 2D field (reconstruct.py, metrics.py) ---------
+    rec = load_reference_module(ref_root, "python/tira/tensors_lib/reconstruct.py", "tira_ref_reconstruct")
+    met = load_reference_module(ref_root, "python/tira/tensors_lib/metrics.py", "tira_ref_metrics")
+    fx = {}
+    rng = np.random.default_rng(21)
+    H, W = 40, 44
+    img = np.zeros((H, W))
+    yy, xx = np.mgrid[0:H, 0:W]
+    for _ in range(4):                       # a few rings and bars: closed curves give holes to fill
+        cy, cx, r = rng.uniform(8, 32), rng.uniform(8, 36), rng.uniform(4, 9)
+        img[np.abs(np.hypot(yy - cy, xx - cx) - r) < 1.0] = 1.0
+    img[5:7, 3:40] = 1.0
+    img += rng.normal(0, 0.05, img.shape)
+    gy, gx = np.gradient(img)
+    T = np.stack([np.stack([gx * gx, gx * gy], -1), np.stack([gx * gy, gy * gy], -1)], -2)
+    T32 = T.astype(np.float32)
+    I = flat4(T32.astype(np.float64)).reshape(H, W, 4)
+    fx["I"] = I
+    V = O.tensorvote2(I, sigma1=2.0, sigma2=0.0, power=1, w=13, samples=20, use_ref=True)
+    V = V.reshape(H, W, 2, 2).astype(np.float32)
+    fx["V"] = V.reshape(H, W, 4)
+    fx["saliency"] = rec.stick_saliency(V)
+    fx["otsu"] = np.float64(rec._otsu_threshold(fx["saliency"].ravel()))
+    fx["mask_otsu"] = rec.saliency_threshold(V)
+    fx["mask_fixed"] = rec.saliency_threshold(V, threshold=float(np.median(fx["saliency"])))
+    fx["mask_fill_r0"] = rec.saliency_threshold(V, fill=True)
+    fx["mask_fill_r2"] = rec.saliency_threshold(V, fill=True, close_radius=2)
+    # the sweep's objective: simf of a target against votes of the field at several parameter sets
+    G = O.tensorvote2(I, sigma1=3.0, sigma2=1.0, power=1, w=19, samples=20, use_ref=True)
+    G = G.reshape(H, W, 2, 2).astype(np.float32)
+    fx["G"] = G.reshape(H, W, 4)
+    params = np.array([[1.5, 0.0, 1], [3.0, 1.0, 1], [2.5, 0.5, 2], [4.2, 3.0, 3]], np.float64)
+    fx["sweep_params"] = params
+    vals = []
+    for s1, s2, pw in params:
+        w = 2 * int(3 * max(s1, s2)) + 1
+        B = O.tensorvote2(I, sigma1=s1, sigma2=s2, power=int(pw), w=w, samples=20, use_ref=True)
+        vals.append(met.simf(G, B.reshape(H, W, 2, 2).astype(np.float32)))
+    fx["sweep_simf"] = np.array(vals, np.float64)
+    np.savez_compressed(os.path.join(HERE, "reconstruct_reference.npz"), **fx)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

@@ -1,0 +1,115 @@
+"""The surrogate on the GPU: its training samples against the oracle's plain
+integral, its training kernels' gradients against the FP64 CPU MLP, its
+tensor-core inference against the oracle forward, training, and the 3D
+vote with the plate by the network, the exact closed form and the plain
+64-orientation integral."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def S():
+    from tiralib_gb300 import surrogate
+    return surrogate
+
+
+@pytest.fixture(scope="module")
+def trained(S):
+    """A network trained briefly (the tests use it for its behaviour, not
+    for the accuracy of a full training run)."""
+    X, T = S.samples(1 << 18, seed=11)
+    p = S.init_params(0)
+    hist = S.train(p, X, T, batch=4096, steps=4000, lr=3e-3)
+    return p, hist
+
+
+def test_samples_are_the_plain_integral(S):
+    X, T = S.samples(3000, seed=5)
+    np.testing.assert_allclose(np.linalg.norm(X[:, :3], axis=1), 1.0, atol=1e-5)
+    np.testing.assert_allclose(np.linalg.norm(X[:, 3:6], axis=1), 1.0, atol=1e-5)
+    assert set(np.unique(X[:, 6])) <= {0.0, 1.0} and 0.3 < X[:, 6].mean() < 0.7
+    ref = np.array([O.surrogate_target(x[:3], x[3:6], int(x[6])) for x in X[:400]])
+    np.testing.assert_allclose(T[:400, :6], ref, rtol=0, atol=2e-6)
+    assert np.all(T[:, 6:] == 0) and np.all(X[:, 7] == 0)
+
+
+def test_training_gradient_matches_fp64_mlp(S):
+    rng = np.random.default_rng(2)
+    p = S.init_params(4) + rng.normal(0, 0.02, S.param_count()).astype(np.float32)
+    p[S.layout()[-1][1] + 6:] = 0.0
+    X, T = S.samples(256, seed=9)
+    g, loss = S.grad(p, X, T)
+    loss_ref, g_ref, _ = O.mlp_loss_grad(p.astype(np.float64), X, T, quant=True)
+    assert loss == pytest.approx(loss_ref, rel=1e-3)
+    # FP32 accumulation and rare flips of a bf16 rounding against the FP64 oracle
+    assert np.linalg.norm(g - g_ref) <= 2e-3 * np.linalg.norm(g_ref)
+    for name, off, shape in S.layout():
+        n = int(np.prod(shape))
+        blk, ref = g[off:off + n], g_ref[off:off + n]
+        assert np.linalg.norm(blk - ref) <= 5e-3 * max(np.linalg.norm(ref), 1e-8), name
+
+
+def test_tensor_core_inference_matches_fp64_forward(S):
+    rng = np.random.default_rng(3)
+    p = S.init_params(7)
+    X, T = S.samples(5000, seed=3)
+    Y = S.evaluate(p, X)
+    _, _, Yref = O.mlp_loss_grad(p.astype(np.float64), X, T, quant=True)
+    err = np.abs(Y[:, :6] - Yref[:, :6])
+    scale = np.abs(Yref[:, :6]).max()
+    assert np.median(err) <= 2e-3 * scale and err.max() <= 3e-2 * scale
+
+
+def test_training_reduces_the_loss(S, trained):
+    p, hist = trained
+    assert np.all(np.isfinite(hist))
+    assert hist[-50:].mean() < 0.1 * hist[:10].mean()
+    X, T = S.samples(20000, seed=77)       # held-out pairs
+    Y = S.evaluate(p, X)
+    rel = np.linalg.norm(Y[:, :6] - T[:, :6]) / np.linalg.norm(T[:, :6])
+    print(f"held-out relative error of the briefly trained network: {rel:.3g}")
+    assert rel < 0.08
+
+
+def _field(seed, shape=(20, 22, 24)):
+    import tiralib_gb300 as tv
+    rng = np.random.default_rng(seed)
+    vol = rng.normal(size=shape).astype(np.float32)
+    return tv.structure_tensor3(vol, 1.0, mode="same", layout="mat3")
+
+
+@pytest.mark.parametrize("ball", [False, True])
+def test_closed_and_plain64_modes_are_the_exact_vote(S, ball):
+    import tiralib_gb300 as tv
+    F = _field(1)
+    closed, _, _, _ = S.vote3(F, 2.0, mode="closed", ball=ball)
+    plain, _, _, _ = S.vote3(F, 2.0, mode="plain64", ball=ball)
+    ref, _, _ = tv.vote3(F, 2.0, 0.0, samples=20, ball=ball)
+    u = [0, 1, 2, 4, 5, 8]
+    scale = np.abs(ref.reshape(-1, 9)[:, u]).max()
+    assert np.abs(closed - ref).max() <= 1e-5 * scale
+    assert np.abs(plain - ref).max() <= 1e-5 * scale
+
+
+def test_surrogate_vote_and_its_judge(S, trained):
+    import tiralib_gb300 as tv
+    p, _ = trained
+    F = _field(2)
+    exact, _, _, _ = S.vote3(F, 2.0, mode="closed", ball=True)
+    # tol = 0: every CTA fails the judge and is voted exactly
+    strict, _, _, st = S.vote3(F, 2.0, params=p, mode="surrogate", tol=0.0, ball=True)
+    assert st[0] > 0 and st[1] == st[0]
+    assert np.abs(strict - exact).max() <= 1e-5 * np.abs(exact).max()
+    # a loose tolerance keeps the network's plate everywhere
+    loose, _, _, st = S.vote3(F, 2.0, params=p, mode="surrogate", tol=1e9, ball=True)
+    assert st[1] == 0
+    rel = np.linalg.norm(loose - exact) / np.linalg.norm(exact)
+    print(f"surrogate vote relative error (briefly trained network): {rel:.3g}")
+    assert rel < 0.05
+    # without the network the mode is refused
+    with pytest.raises(tv.TvgbError):
+        S.vote3(F, 2.0, params=None, mode="surrogate")

@@ -189,3 +189,26 @@ def test_fp64_oracle_close_to_fp32_reference(golden):
     f64 = O.tensorvote3_f64(T, 1.5, 0.0, 5, 1).reshape(-1, 6)
     ref = g["tk_s15_n20"].reshape(-1, 9)[:, UNIQUE9]
     assert rel(ref, f64) < 1e-4
+
+
+def test_consumers_match_reference(golden):
+    """The oracle's restatement of reconstruct.py / metrics.py against the
+    reference's own outputs (tests/golden/reconstruct_reference.npz)."""
+    g = golden("reconstruct_reference.npz")
+    H, W = g["V"].shape[:2]
+    V = g["V"].reshape(H, W, 2, 2)
+    s = O.stick_saliency(V)
+    np.testing.assert_allclose(s, g["saliency"], rtol=0, atol=1e-6 * float(g["saliency"].max()))
+    assert abs(O.otsu_threshold(g["saliency"].ravel()) - float(g["otsu"])) < 1e-12
+    sal = g["saliency"]
+    assert np.array_equal(sal > float(g["otsu"]), g["mask_otsu"])
+    assert np.array_equal(O.saliency_threshold(V, fill=True), g["mask_fill_r0"]) or \
+        np.abs(s - float(g["otsu"])).min() < 1e-6
+    assert np.array_equal(O.saliency_threshold(V, fill=True, close_radius=2), g["mask_fill_r2"]) or \
+        np.abs(s - float(g["otsu"])).min() < 1e-6
+    G = g["G"].reshape(H, W, 2, 2)
+    I = g["I"]
+    for (s1, s2, pw), ref in zip(g["sweep_params"], g["sweep_simf"]):
+        w = 2 * int(3 * max(s1, s2)) + 1
+        B = O.tensorvote2(I, s1, s2, int(pw), w, samples=20).reshape(H, W, 2, 2)
+        assert abs(O.simf(G, B) - ref) <= 1e-5 * max(abs(ref), 1e-3)

@@ -1,0 +1,60 @@
+"""The surrogate's CPU side: the FP64 MLP oracle's gradient against finite
+differences, its training target (the plain 64-orientation integral)
+against the closed-form plate and ball, and the weights file."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+
+def test_oracle_gradient_matches_finite_differences():
+    rng = np.random.default_rng(0)
+    P = rng.normal(size=O.mlp_param_count()) * 0.2
+    X = rng.normal(size=(6, 8))
+    X[:, 7] = 0.0
+    T = rng.normal(size=(6, 8))
+    _, g, _ = O.mlp_loss_grad(P, X, T, quant=False)
+    h = 1e-6
+    for i in rng.choice(len(P), 40, replace=False):
+        Pp, Pm = P.copy(), P.copy()
+        Pp[i] += h
+        Pm[i] -= h
+        fd = (O.mlp_loss_grad(Pp, X, T, False)[0] - O.mlp_loss_grad(Pm, X, T, False)[0]) / (2 * h)
+        assert abs(fd - g[i]) <= 1e-5 * max(abs(fd), 1e-3)
+
+
+def test_target_is_the_exact_plate_and_ball():
+    """64 orientations integrate the degree-4 integrand exactly: the target
+    equals the closed forms (sigma2 = 0, Gaussian factored out)."""
+    rng = np.random.default_rng(1)
+    iu = [(0, 0), (0, 1), (0, 2), (1, 1), (1, 2), (2, 2)]
+    for _ in range(20):
+        d = rng.normal(size=3)
+        d /= np.linalg.norm(d)
+        n = rng.normal(size=3)
+        n /= np.linalg.norm(n)
+        R = np.eye(3) - 2 * np.outer(d, d)
+        m, p = R @ n, (np.eye(3) - np.outer(n, n)) @ d
+        plate = (0.5 - p @ p / 8) * (np.eye(3) - np.outer(m, m)) - 0.25 * np.outer(R @ p, R @ p)
+        ball = (1 / 3 - 1 / 15) * np.eye(3) - (2 / 15) * np.outer(d, d)
+        np.testing.assert_allclose(O.surrogate_target(d, n, 1), [plate[i, j] for i, j in iu], atol=1e-14)
+        np.testing.assert_allclose(O.surrogate_target(d, n, 0), [ball[i, j] for i, j in iu], atol=1e-14)
+
+
+def test_weights_file_roundtrip_and_checksum(tmp_path):
+    from tiralib_gb300 import surrogate as S
+    p = S.init_params(3)
+    assert p.size == S.param_count() == O.mlp_param_count()
+    W1 = p[:512].reshape(64, 8)
+    assert np.all(W1[:, 7] == 0)
+    f = os.path.join(tmp_path, "net.bin")
+    S.save(f, p, "sigma2 = 0, power 1")
+    q, note = S.load(f)
+    assert np.array_equal(p, q) and note == "sigma2 = 0, power 1"
+    blob = bytearray(open(f, "rb").read())
+    blob[-5] ^= 0x40
+    open(f, "wb").write(bytes(blob))
+    with pytest.raises(ValueError, match="checksum"):
+        S.load(f)

@@ -36,6 +36,20 @@ SIGNATURES = {
     "tvgb_version": (_I, []),
     "tvgb_launch_count": (ctypes.c_ulonglong, []),
     "tvgb_memory_stats": (_I, [_P, _P, ctypes.c_int]),
+    "tvgb_surrogate_param_count": (_I, []),
+    "tvgb_surrogate_samples": (_I, [_SZ, ctypes.c_ulonglong, _P, _P, _P]),
+    "tvgb_surrogate_grad": (_I, [_P, _P, _P, _I, _P, _P, _P]),
+    "tvgb_surrogate_train": (_I, [_P, _P, _P, _SZ, _I, _I, _F, _P, _P]),
+    "tvgb_surrogate_eval": (_I, [_P, _P, _SZ, _P, _P]),
+    "tvgb_vote3_surrogate": (_I, [_P, _I, _U, _U, _U, ctypes.POINTER(Vote3Params), _P, _I, _F, _P, _I, _P, _P, _I,
+                                  _P, _P]),
+    "tvgb_stick_saliency2": (_I, [_P, _SZ, _P, _P]),
+    "tvgb_otsu_threshold": (_I, [_P, _SZ, _P, _P]),
+    "tvgb_saliency_threshold2": (_I, [_P, ctypes.c_uint, ctypes.c_uint, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                      ctypes.c_int, _P, _P, _P]),
+    "tvgb_simf2": (_I, [_P, _P, _SZ, _P, _P]),
+    "tvgb_tensorvote_sweep": (_I, [_P, _P, ctypes.c_uint, ctypes.c_uint, _P, ctypes.c_int, ctypes.c_uint, ctypes.c_int,
+                                   _P, _P, _P]),
     "tvgb_evals3_symmetric": (_I, [_P, _SZ, _P, _P]),
     "tvgb_evecs3spherical_symmetric": (_I, [_P, _P, _SZ, _P, _P]),
     "tvgb_evals2_symmetric": (_I, [_P, _SZ, _P, _P]),

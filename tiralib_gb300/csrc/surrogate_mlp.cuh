@@ -1,0 +1,121 @@
+// The plate / ball vote surrogate's network on the tensor cores.
+//
+// MLP 7 -> 64 -> 64 -> 64 -> 6 (GELU) from (offset direction o / |o|, plate
+// normal n, flag 1 plate / 0 ball), inputs padded to 8 (K = 16 for the
+// first MMA), outputs padded to 8.  Weights and activations are bfloat16,
+// accumulation FP32: mma.sync.m16n8k16 (BF16) with each warp carrying 16
+// samples.  A layer's FP32 accumulators, after bias (loaded as the
+// accumulator's initial value) and GELU, are packed to bfloat16 and become
+// the next layer's A fragments in the same registers: the accumulator of
+// n-tiles 2k and 2k+1 is exactly the A fragment of k-tile k, so the whole
+// network runs without touching shared memory for activations.  Weights are
+// pre-arranged per (layer, k-tile, n-tile, lane) as the B fragment each lane
+// holds (two 32-bit registers), so each MMA needs one 64-bit shared load.
+//
+// Parameter layout (FP32 master copy):
+//   W1[64][8] b1[64] W2[64][64] b2[64] W3[64][64] b3[64] W4[8][64] b4[8]
+// with W[out][in]; W1[.][7], W4[6..7][.] and b4[6..7] stay zero.
+#pragma once
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+namespace tvgb {
+
+constexpr int SUR_IN = 8, SUR_H = 64, SUR_OUT = 8;
+constexpr int SUR_W1 = 0;
+constexpr int SUR_B1 = SUR_W1 + SUR_H * SUR_IN;
+constexpr int SUR_W2 = SUR_B1 + SUR_H;
+constexpr int SUR_B2 = SUR_W2 + SUR_H * SUR_H;
+constexpr int SUR_W3 = SUR_B2 + SUR_H;
+constexpr int SUR_B3 = SUR_W3 + SUR_H * SUR_H;
+constexpr int SUR_W4 = SUR_B3 + SUR_H;
+constexpr int SUR_B4 = SUR_W4 + SUR_OUT * SUR_H;
+constexpr int SUR_NPARAM = SUR_B4 + SUR_OUT;     // 9416
+// B fragments: layer 1 (1 k-tile x 8 n-tiles), 2 and 3 (4 x 8), 4 (4 x 1)
+constexpr int SUR_F1 = 0, SUR_F2 = 8, SUR_F3 = 40, SUR_F4 = 72, SUR_NFRAG = 76;
+constexpr int SUR_NBIAS = 3 * SUR_H + SUR_OUT;   // b1 b2 b3 b4
+
+constexpr float GELU_K = 0.7978845608028654f;    // sqrt(2 / pi)
+constexpr float GELU_A = 0.044715f;
+
+__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
+    const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);   // .x (low half) = lo
+    return *reinterpret_cast<const uint32_t*>(&v);
+}
+
+__device__ __forceinline__ float tanh_fast(float x) {
+    float y;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// GELU, tanh form, with the hardware tanh approximation (inference)
+__device__ __forceinline__ float gelu_fast(float z) {
+    const float u = GELU_K * fmaf(GELU_A * z, z * z, z);
+    const float h = 0.5f * z;
+    return fmaf(h, tanh_fast(u), h);
+}
+
+__device__ __forceinline__ void mma_bf16_16816(float (&c)[4], const uint32_t (&a)[4], uint2 b) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
+        "{%0, %1, %2, %3};"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b.x), "r"(b.y));
+}
+
+// One 16-sample tile through the network.  a_in: this lane's A fragment of
+// the 16 x 16 input (rows g, g+8; columns 2 t, 2 t + 1 in registers 0 / 1,
+// columns 8 + 2 t, ... in registers 2 / 3, which are zero: 8 inputs).
+// frag: the 76 x 32 B fragments (shared memory), bias: b1 b2 b3 b4.
+// Returns the lane's output accumulator: rows g (out[0..1]) and g + 8
+// (out[2..3]), output columns 2 t, 2 t + 1, with g = lane / 4, t = lane % 4.
+__device__ __forceinline__ void sur_mlp16(const uint2* __restrict__ frag, const float* __restrict__ bias,
+                                          const uint32_t (&a_in)[4], float (&out)[4]) {
+    const int lane = threadIdx.x & 31, t = lane & 3;
+    float c[8][4];
+    uint32_t a[4][4];
+    // layer 1
+#pragma unroll
+    for (int nt = 0; nt < 8; ++nt) {
+        const float b0 = bias[nt * 8 + 2 * t], b1 = bias[nt * 8 + 2 * t + 1];
+        c[nt][0] = b0; c[nt][1] = b1; c[nt][2] = b0; c[nt][3] = b1;
+        mma_bf16_16816(c[nt], a_in, frag[(SUR_F1 + nt) * 32 + lane]);
+    }
+#pragma unroll
+    for (int layer = 0; layer < 2; ++layer) {
+#pragma unroll
+        for (int kt = 0; kt < 4; ++kt) {
+            a[kt][0] = pack_bf16x2(gelu_fast(c[2 * kt][0]), gelu_fast(c[2 * kt][1]));
+            a[kt][1] = pack_bf16x2(gelu_fast(c[2 * kt][2]), gelu_fast(c[2 * kt][3]));
+            a[kt][2] = pack_bf16x2(gelu_fast(c[2 * kt + 1][0]), gelu_fast(c[2 * kt + 1][1]));
+            a[kt][3] = pack_bf16x2(gelu_fast(c[2 * kt + 1][2]), gelu_fast(c[2 * kt + 1][3]));
+        }
+        const int fbase = layer == 0 ? SUR_F2 : SUR_F3;
+        const float* bl = bias + SUR_H * (layer + 1);
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt) {
+            const float b0 = bl[nt * 8 + 2 * t], b1 = bl[nt * 8 + 2 * t + 1];
+            c[nt][0] = b0; c[nt][1] = b1; c[nt][2] = b0; c[nt][3] = b1;
+#pragma unroll
+            for (int kt = 0; kt < 4; ++kt) mma_bf16_16816(c[nt], a[kt], frag[(fbase + kt * 8 + nt) * 32 + lane]);
+        }
+    }
+#pragma unroll
+    for (int kt = 0; kt < 4; ++kt) {
+        a[kt][0] = pack_bf16x2(gelu_fast(c[2 * kt][0]), gelu_fast(c[2 * kt][1]));
+        a[kt][1] = pack_bf16x2(gelu_fast(c[2 * kt][2]), gelu_fast(c[2 * kt][3]));
+        a[kt][2] = pack_bf16x2(gelu_fast(c[2 * kt + 1][0]), gelu_fast(c[2 * kt + 1][1]));
+        a[kt][3] = pack_bf16x2(gelu_fast(c[2 * kt + 1][2]), gelu_fast(c[2 * kt + 1][3]));
+    }
+    const float* b4 = bias + 3 * SUR_H;
+    out[0] = b4[2 * t]; out[1] = b4[2 * t + 1]; out[2] = out[0]; out[3] = out[1];
+#pragma unroll
+    for (int kt = 0; kt < 4; ++kt) mma_bf16_16816(out, a[kt], frag[(SUR_F4 + kt) * 32 + lane]);
+}
+
+// Host-side: the B fragments and bias vector of a parameter vector (FP32
+// master copy, layout above).  frag: SUR_NFRAG * 32 uint2, bias: SUR_NBIAS floats.
+void sur_make_fragments(const float* params, uint2* frag, float* bias);
+
+}  // namespace tvgb

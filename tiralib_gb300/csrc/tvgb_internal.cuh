@@ -17,6 +17,14 @@ void structure_tensor3_dims(unsigned s0, unsigned s1, unsigned s2, float sigma, 
 int vote3_device(const float* in, int in_layout, unsigned s0, unsigned s1, unsigned s2, const tvgb_vote3_params& p,
                  float* out, int out_layout, float* evals3, float* evecs, int evec_format, cudaStream_t s);
 
+// reconstruct.cu: SIMF of two (n, 4) fields into acc[0..2] = (<A,B>, <B,B>, sum of norms)
+int simf2_device(const float4* A, const float4* B, size_t n, double* acc3, cudaStream_t s);
+
+// surrogate.cu: the network's tensor-core form from a parameter vector
+// (host or device), and its evaluation on n inputs (n x 8 floats)
+int sur_upload(const float* params, uint2* frag_dev, float* bias_dev, cudaStream_t s);
+int sur_eval_device(const uint2* frag, const float* bias, const float* X, size_t n, float* Y, cudaStream_t s);
+
 // window rule of the reference's Python layer (tensorvote_tk.cu:88-95)
 inline unsigned auto_window(float s1, float s2) {
     const float sm = s2 > s1 ? s2 : s1;

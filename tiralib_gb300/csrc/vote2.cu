@@ -15,7 +15,9 @@
 // reference's float arithmetic (it is O(w^2 samples) and tiny).
 #include "tvgb_internal.cuh"
 #include "eig_device.cuh"
+#include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <vector>
 
 namespace tvgb {
@@ -142,6 +144,77 @@ __global__ void __launch_bounds__(V2X * V2Y) k_vote2_tk(const float4* __restrict
     if (x < s1 && y < s0) out[size_t(y) * s1 + x] = make_float4(sa + pa, sb + pb, sb + pb, sc + pc);
 }
 
+// Staged variant for windows whose voter tile fits in shared memory: the
+// CTA's 32 x 32 receivers (4 rows per thread) read their voters from a
+// (32 + 2 h) x (32 + 2 h) tile staged once, zero outside the image, so the
+// table loop has no bounds checks and each table entry (a warp-uniform
+// broadcast) serves 4 receivers.  h bounds |du|, |dv| over the table.
+template <int V2R, bool STICK, bool PLATE, bool P1>
+__global__ void __launch_bounds__(V2X * V2Y) k_vote2_tks(const float4* __restrict__ V, const Nb2* __restrict__ nb,
+                                                          int nbc, int s0, int s1, int h, float eta_s, unsigned power,
+                                                          float4* __restrict__ out) {
+    extern __shared__ __align__(16) float4 sm2[];
+    Nb2* snb = reinterpret_cast<Nb2*>(sm2);                       // NB_CHUNK entries
+    float4* tile = sm2 + NB_CHUNK * sizeof(Nb2) / sizeof(float4);  // TW x TW voters
+    const int TW = V2X + 2 * h;
+    const int x0 = blockIdx.x * V2X, y0 = blockIdx.y * (V2Y * V2R);
+    const int tid = threadIdx.y * V2X + threadIdx.x;
+    for (int e = tid; e < TW * TW; e += V2X * V2Y) {
+        const int r = e / TW, c = e - r * TW;
+        const int gy = y0 - h + r, gx = x0 - h + c;
+        tile[e] = ((unsigned)gy < (unsigned)s0 && (unsigned)gx < (unsigned)s1) ? __ldg(V + size_t(gy) * s1 + gx)
+                                                                               : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    float sa[V2R], sb[V2R], sc[V2R], pa[V2R], pb[V2R], pc[V2R];
+#pragma unroll
+    for (int j = 0; j < V2R; ++j) { sa[j] = sb[j] = sc[j] = pa[j] = pb[j] = pc[j] = 0.0f; }
+    // receiver j of this thread: (x0 + tx, y0 + ty + 8 j); its voter at (du, dv) is tile[ty + 8 j + h + dv][tx + h + du]
+    const float4* base = tile + (threadIdx.y + h) * TW + threadIdx.x + h;
+    for (int c0 = 0; c0 < nbc; c0 += NB_CHUNK) {
+        const int cn = min(NB_CHUNK, nbc - c0);
+        __syncthreads();
+        for (int i = tid; i < cn; i += V2X * V2Y) snb[i] = nb[c0 + i];
+        __syncthreads();
+#pragma unroll 2
+        for (int k = 0; k < cn; ++k) {
+            const Nb2& e = snb[k];
+            const float4* vp = base + e.dv * TW + e.du;
+#pragma unroll
+            for (int j = 0; j < V2R; ++j) {
+                const float4 v = vp[j * V2Y * TW];
+                if (STICK) {
+                    const float qTd = fmaf(v.x, e.dx, v.y * e.dy);
+                    const float q2 = qTd * qTd;
+                    float D;
+                    if (P1) D = fmaf(e.c1, 1.0f - q2, e.c2 * q2);
+                    else {
+                        const float t1 = 1.0f - q2, t2 = q2;
+                        float e1 = t1, e2 = t2;
+                        for (unsigned i = 1; i < power; ++i) { e1 *= t1; e2 *= t2; }
+                        D = e.c1 * e1 + e.c2 * e2;
+                    }
+                    const float Rqx = fmaf(e.Ra, v.x, e.Rb * v.y), Rqy = fmaf(e.Rb, v.x, e.Rc * v.y);
+                    const float f = D * v.z;
+                    const float fx = f * Rqx;
+                    sa[j] = fmaf(fx, Rqx, sa[j]); sb[j] = fmaf(fx, Rqy, sb[j]); sc[j] = fmaf(f * Rqy, Rqy, sc[j]);
+                }
+                if (PLATE) {   // v.w = 0 outside the image and for zero plates
+                    pa[j] = fmaf(v.w, e.Va, pa[j]); pb[j] = fmaf(v.w, e.Vb, pb[j]); pc[j] = fmaf(v.w, e.Vc, pc[j]);
+                }
+            }
+        }
+    }
+    const int x = x0 + threadIdx.x;
+    if (x >= s1) return;
+#pragma unroll
+    for (int j = 0; j < V2R; ++j) {
+        const int y = y0 + threadIdx.y + V2Y * j;
+        if (y >= s0) break;
+        const float a = fmaf(eta_s, sa[j], pa[j]), b = fmaf(eta_s, sb[j], pb[j]), c = fmaf(eta_s, sc[j], pc[j]);
+        out[size_t(y) * s1 + x] = make_float4(a, b, b, c);
+    }
+}
+
 // atv (2D, tensorvote.h:225) with atv_H (:161); out [a, b, c]
 __device__ __forceinline__ void atv2_pair(float l0, float l1, float e0x, float e0y, float e1x, float e1y, float rx,
                                           float ry, float sigma, float& Va, float& Vb, float& Vc) {
@@ -190,11 +263,85 @@ __global__ void __launch_bounds__(V2X * V2Y) k_vote2_atv(const float4* __restric
     out[size_t(y) * s1 + x] = make_float4(oa, ob, ob, oc);
 }
 
+// One TK vote of prepared voter records V (k_prep2) into out: the
+// Neighbor2D table is the caller's (host or device) or built here with the
+// reference's float steps; the staged kernel runs whenever the table is on
+// the host and its voter tile fits in shared memory.
+static int vote2_tk_launch(const float4* V, const Nb2* host_or_dev_nb, int nbc, float s1, float s2, int power,
+                           unsigned w, unsigned S0, unsigned S1, bool stick, bool plate, unsigned samples, float4* out,
+                           cudaStream_t st) {
+    const bool use_plate = plate && samples > 0;
+    std::vector<Nb2> table;
+    const Nb2* nbp = host_or_dev_nb;
+    if (!nbp) {
+        table.resize(size_t(w) * w);
+        nbc = build_table(int(w), s1, s2, unsigned(power), samples, stick, use_plate, table.data());
+        nbp = table.data();
+    }
+    DevArray dnb;
+    TVGB_TRY(dnb.in(nbp, size_t(nbc) * sizeof(Nb2), st));
+    const unsigned p = power < 1 ? 1u : unsigned(power);
+    const float eta_s = stick_norm_2d_h(s1, s2, p);
+    int h = -1;
+    if (!is_device_ptr(nbp)) {
+        h = 0;
+        for (int i = 0; i < nbc; ++i) h = std::max(h, std::max(std::abs(nbp[i].du), std::abs(nbp[i].dv)));
+    }
+    const size_t tw = size_t(V2X) + 2 * size_t(h < 0 ? 0 : h);
+    const size_t smem_s = NB_CHUNK * sizeof(Nb2) + tw * tw * sizeof(float4);
+    dim3 grid(ceil_div(S1, V2X), ceil_div(S0, V2Y)), blk(V2X, V2Y);
+    {
+        KernelTimer kt_("k_vote2_tk", st);
+        if (h >= 0 && smem_s <= 200 * 1024) {
+            // receivers per thread: 4 (each table entry serves 4 receivers) measured fastest
+            // even where it leaves the GPU under one wave (512^2: 0.095 ms vs 0.117 / 0.133 ms
+            // for 2 / 1)
+#ifdef TVGB_V2R
+            const int R = TVGB_V2R;
+#else
+            const int R = 4;
+#endif
+            const void* fn = nullptr;
+#define TVGB_TKS(RR)                                                                                          \
+    if (R == RR) {                                                                                              \
+        if (stick && use_plate) fn = p == 1 ? (const void*)k_vote2_tks<RR, true, true, true>                   \
+                                            : (const void*)k_vote2_tks<RR, true, true, false>;                 \
+        else if (stick) fn = p == 1 ? (const void*)k_vote2_tks<RR, true, false, true>                          \
+                                    : (const void*)k_vote2_tks<RR, true, false, false>;                        \
+        else fn = (const void*)k_vote2_tks<RR, false, true, true>;                                             \
+    }
+            TVGB_TKS(1) TVGB_TKS(2) TVGB_TKS(4)
+#undef TVGB_TKS
+            TVGB_CHECK_ARG(fn, "2D vote: no kernel for %d receivers per thread", R);
+            TVGB_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem_s)));
+            dim3 gs(ceil_div(S1, V2X), ceil_div(S0, unsigned(V2Y * R)));
+            const float4* vp = V;
+            const Nb2* tp = dnb.get<Nb2>();
+            int nbc_ = nbc, s0_ = int(S0), s1_ = int(S1), h_ = h;
+            float eta_ = eta_s;
+            unsigned p_ = p;
+            float4* op = out;
+            void* args[] = {&vp, &tp, &nbc_, &s0_, &s1_, &h_, &eta_, &p_, &op};
+            TVGB_CUDA(cudaLaunchKernel(fn, gs, blk, args, smem_s, st));
+        } else if (stick && use_plate) {
+            k_vote2_tk<true, true><<<grid, blk, 0, st>>>(V, dnb.get<Nb2>(), nbc, int(S0), int(S1), eta_s, p, out);
+        } else if (stick) {
+            k_vote2_tk<true, false><<<grid, blk, 0, st>>>(V, dnb.get<Nb2>(), nbc, int(S0), int(S1), eta_s, p, out);
+        } else {
+            k_vote2_tk<false, true><<<grid, blk, 0, st>>>(V, dnb.get<Nb2>(), nbc, int(S0), int(S1), eta_s, p, out);
+        }
+        kt_.stop();
+    }
+    TVGB_LAUNCHED();
+    if (!host_or_dev_nb) TVGB_CUDA(cudaStreamSynchronize(st));   // the host table must outlive its copy
+    return TVGB_OK;
+}
+
 static int vote2_impl(float* t_out, const float* t_in, const Nb2* host_or_dev_nb, int nbc, float s1, float s2,
                       int power, unsigned w, unsigned S0, unsigned S1, bool stick, bool plate, unsigned samples,
                       bool is_atv, cudaStream_t st) {
     const size_t n = size_t(S0) * S1;
-    DevArray din, dout, dnb;
+    DevArray din, dout;
     TVGB_TRY(din.in(t_in, n * 16, st));
     TVGB_TRY(dout.out(t_out, n * 16, st));
     TVGB_CHECK_ARG(reinterpret_cast<uintptr_t>(din.dev) % 16 == 0 && reinterpret_cast<uintptr_t>(dout.dev) % 16 == 0,
@@ -229,40 +376,11 @@ static int vote2_impl(float* t_out, const float* t_in, const Nb2* host_or_dev_nb
         }
         TVGB_LAUNCHED();
     } else {
-        const bool use_plate = plate && samples > 0;
-        std::vector<Nb2> table;
-        const Nb2* nbp = host_or_dev_nb;
-        if (!nbp) {
-            table.resize(size_t(w) * w);
-            nbc = build_table(int(w), s1, s2, unsigned(power), samples, stick, use_plate, table.data());
-            nbp = table.data();
-        }
-        TVGB_TRY(dnb.in(nbp, size_t(nbc) * sizeof(Nb2), st));
-        const unsigned p = power < 1 ? 1u : unsigned(power);
-        const float eta_s = stick_norm_2d_h(s1, s2, p);
-        if (stick && use_plate)
-            {
-                KernelTimer kt_("k_vote2_tk", st);
-                k_vote2_tk<true, true><<<grid, blk, 0, st>>>(sv.get<float4>(), dnb.get<Nb2>(), nbc, int(S0), int(S1), eta_s, p, dout.get<float4>());
-                kt_.stop();
-            }
-        else if (stick)
-            {
-                KernelTimer kt_("k_vote2_tk", st);
-                k_vote2_tk<true, false><<<grid, blk, 0, st>>>(sv.get<float4>(), dnb.get<Nb2>(), nbc, int(S0), int(S1), eta_s, p, dout.get<float4>());
-                kt_.stop();
-            }
-        else
-            {
-                KernelTimer kt_("k_vote2_tk", st);
-                k_vote2_tk<false, true><<<grid, blk, 0, st>>>(sv.get<float4>(), dnb.get<Nb2>(), nbc, int(S0), int(S1), eta_s, p, dout.get<float4>());
-                kt_.stop();
-            }
-        TVGB_LAUNCHED();
-        if (!nbp || !host_or_dev_nb) TVGB_CUDA(cudaStreamSynchronize(st));   // the host table must outlive its copy
+        TVGB_TRY(vote2_tk_launch(sv.get<float4>(), host_or_dev_nb, nbc, s1, s2, power, w, S0, S1, stick, plate, samples,
+                                 dout.get<float4>(), st));
     }
     TVGB_TRY(dout.finish());
-    return sync_if(din.owned || dout.owned || dnb.owned, st);
+    return sync_if(din.owned || dout.owned, st);
 }
 
 }  // namespace tvgb
@@ -311,6 +429,68 @@ int tvgb_tensorvote_prebuilt(float* t_out, const float* t_in, const void* host_n
     }
     return vote2_impl(t_out, t_in, static_cast<const Nb2*>(host_nb), nb_count, sigma1, sigma2, power, w, shape0, shape1,
                       stick != 0, plate != 0, samples, false, as_stream(stream));
+}
+
+// Parameter sweep of the TK vote (the objective evaluations of tiralib's
+// optimize_tk, python/tira/tensors_lib/optimize.py:256-279): K parameter
+// sets (sigma1, sigma2, power) against one input field and one target field
+// G.  The input is solved once; each set gets its window
+// (optimize.py:_w_from_sigma), its Neighbor2D table, one vote and the SIMF of
+// G against the voted field (metrics.py:37).  simf[k] receives it; t_out, if
+// given, receives the K voted fields.
+int tvgb_tensorvote_sweep(const float* t_in, const float* G, unsigned shape0, unsigned shape1, const double* params,
+                          int K, unsigned samples, int plate, double* simf, float* t_out, void* stream) {
+    TVGB_CHECK_ARG(t_in && G && params && simf, "tvgb_tensorvote_sweep: NULL pointer");
+    TVGB_CHECK_ARG(K >= 0, "tvgb_tensorvote_sweep: K must be >= 0");
+    for (int k = 0; k < K; ++k) {
+        TVGB_CHECK_ARG(params[3 * k] > 0.0 && params[3 * k + 1] >= 0.0 && params[3 * k + 2] >= 1.0 &&
+                           params[3 * k] < 1e4 && params[3 * k + 1] < 1e4 && params[3 * k + 2] < 1e4,
+                       "tvgb_tensorvote_sweep: parameter set %d out of range", k);
+    }
+    const size_t n = size_t(shape0) * shape1;
+    if (K == 0) return TVGB_OK;
+    if (n == 0) { for (int k = 0; k < K; ++k) simf[k] = 0.0; return TVGB_OK; }
+    cudaStream_t st = as_stream(stream);
+    DevArray din, dG, dout;
+    TVGB_TRY(din.in(t_in, n * 16, st));
+    TVGB_TRY(dG.in(G, n * 16, st));
+    if (t_out) TVGB_TRY(dout.out(t_out, size_t(K) * n * 16, st));
+    TVGB_CHECK_ARG(reinterpret_cast<uintptr_t>(din.dev) % 16 == 0 && reinterpret_cast<uintptr_t>(dG.dev) % 16 == 0 &&
+                       reinterpret_cast<uintptr_t>(dout.dev) % 16 == 0,
+                   "tvgb_tensorvote_sweep: fields must be 16-byte aligned");
+    Scratch sv, sb, sacc;
+    TVGB_TRY(sv.alloc(n * 16, st));
+    if (!t_out) TVGB_TRY(sb.alloc(n * 16, st));
+    TVGB_TRY(sacc.alloc(size_t(K) * 3 * sizeof(double), st));
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    size_t blocks = (n + 255) / 256;
+    if (blocks > size_t(sms) * 16) blocks = size_t(sms) * 16;
+    {
+        KernelTimer kt_("k_prep2", st);
+        k_prep2<<<unsigned(blocks ? blocks : 1), 256, 0, st>>>(din.get<float4>(), n, sv.get<float4>(), nullptr);
+        kt_.stop();
+    }
+    TVGB_LAUNCHED();
+    for (int k = 0; k < K; ++k) {
+        const double s1d = params[3 * k], s2d = params[3 * k + 1];
+        const int pw = std::max(1, int(params[3 * k + 2]));
+        const double sm = std::max(s1d, s2d);
+        int w = 2 * int(3.0 * sm) + 1;        // optimize.py:9-15
+        if (w < 3) w = 3;
+        if (w % 2 == 0) w += 1;
+        float4* B = t_out ? dout.get<float4>() + size_t(k) * n : sb.get<float4>();
+        TVGB_TRY(vote2_tk_launch(sv.get<float4>(), nullptr, 0, float(s1d), float(s2d), pw, unsigned(w), shape0, shape1,
+                                 true, plate != 0, samples, B, st));
+        TVGB_TRY(simf2_device(dG.get<float4>(), B, n, sacc.get<double>() + 3 * k, st));
+    }
+    std::vector<double> acc(size_t(K) * 3);
+    TVGB_CUDA(cudaMemcpyAsync(acc.data(), sacc.get<double>(), acc.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+    TVGB_TRY(dout.finish());
+    TVGB_CUDA(cudaStreamSynchronize(st));
+    for (int k = 0; k < K; ++k) simf[k] = acc[3 * k + 2] / double(n);
+    return TVGB_OK;
 }
 
 }  // extern "C"

@@ -943,3 +943,463 @@ extern "C" int tvgb_vote3_noalloc(const float* in, int in_layout, unsigned s0, u
     }
     return launch_fast(fa, S, P, B, st);
 }
+
+// ------------------------------------------------------------------ learned plate / ball vote
+// tvgb_vote3_surrogate: the stick vote exact (as k_vote3_fast), the plate
+// vote by one of three rules, chosen so that they can be timed side by side
+// in the same kernel skeleton (one receiver per lane, 32 x 4 receivers per
+// CTA, voters read through L1 / L2):
+//   PLATE_SURROGATE  the MLP of surrogate_mlp.cuh on the tensor cores: for
+//                    each voter offset a warp runs its 32 (receiver, voter)
+//                    pairs as two 16-row tiles; o = 0 is voted exactly.  A
+//                    judge then votes the plate of the CTA's first 32
+//                    receivers exactly; if any of them differs from the
+//                    surrogate by more than tol x the norm of its full voted
+//                    tensor, the whole CTA's plate is recomputed exactly.
+//   PLATE_CLOSED     the exact closed form of k_vote3_fast.
+//   PLATE_PLAIN64    the plain orientation integral with 64 orientations
+//                    (the reference's plate3_numerical_device rule,
+//                    tensorvote.h:2457, basis :2467-2469).
+// The ball vote (lambda0 x the mean unit stick vote over the sphere) depends
+// on the offset only: it is tabulated per offset by the same rule (network
+// with flag 0 / closed form / 8 x 8 sphere rule) and applied per pair.
+#include "surrogate_mlp.cuh"
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+namespace tvgb {
+
+enum { PLATE_SURROGATE = 0, PLATE_CLOSED = 1, PLATE_PLAIN64 = 2 };
+
+struct SurVoteArgs {
+    FastArgs f;
+    const uint2* frag;        // network (PLATE_SURROGATE)
+    const float* bias;
+    const float* ball_tab;    // (2 hw + 1)^3 x 8 floats, or NULL
+    const float* ball_exact;  // the exact ball table (the judge's), PLATE_SURROGATE only
+    float inv_sig;
+    float tol;
+    unsigned* stats;          // [0] CTAs, [1] CTAs whose plate was recomputed exactly
+};
+
+__constant__ float c_cs64[64], c_sn64[64];
+// 8-point Gauss-Legendre rule on [-1, 1] (nodes, weights)
+__constant__ float c_gl8x_v[8] = {-0.9602898564975363f, -0.7966664774136267f, -0.5255324099163290f,
+                                  -0.1834346424956498f, 0.1834346424956498f,  0.5255324099163290f,
+                                  0.7966664774136267f,  0.9602898564975363f};
+__constant__ float c_gl8w_v[8] = {0.1012285362903763f, 0.2223810344533745f, 0.3137066458778873f,
+                                  0.3626837833783620f, 0.3626837833783620f, 0.3137066458778873f,
+                                  0.2223810344533745f, 0.1012285362903763f};
+
+// the plain orientation integral's plate for one pair (sigma2 = 0 rule via the radial table)
+__device__ __forceinline__ void plate_plain64(const float4& B, float ox, float oy, float oz, const float4& ta,
+                                              float L2, float* P) {
+    if (B.w == 0.0f) return;
+    const float n0 = B.x, n1 = B.y, n2 = B.z;
+    float u0, u1, u2;
+    if (fabsf(n2) < 0.999f) { u0 = n1; u1 = -n0; u2 = 0.0f; } else { u0 = 0.0f; u1 = n2; u2 = -n1; }
+    const float iu = rsqrtf(u0 * u0 + u1 * u1 + u2 * u2);
+    u0 *= iu; u1 *= iu; u2 *= iu;
+    const float v0 = n1 * u2 - n2 * u1, v1 = n2 * u0 - n0 * u2, v2 = n0 * u1 - n1 * u0;
+    const float c1 = ta.x, ctg = ta.y, g2 = ta.z;        // c1, (c2 - c1)/|o|^2, 2/|o|^2
+    const float ws = B.w * (1.0f / 64.0f);
+    float a0 = 0, a1 = 0, a2 = 0, a3 = 0, a4 = 0, a5 = 0;
+#pragma unroll 4
+    for (int i = 0; i < 64; ++i) {
+        const float cs = c_cs64[i], sn = c_sn64[i];
+        const float q0 = fmaf(cs, u0, sn * v0), q1 = fmaf(cs, u1, sn * v1), q2 = fmaf(cs, u2, sn * v2);
+        const float qo = fmaf(q0, ox, fmaf(q1, oy, q2 * oz));
+        const float eta = fmaf(ctg, qo * qo, c1);
+        const float k = qo * g2;
+        const float r0 = fmaf(-k, ox, q0), r1 = fmaf(-k, oy, q1), r2 = fmaf(-k, oz, q2);
+        const float t0 = eta * r0, t1 = eta * r1, t2 = eta * r2;
+        a0 = fmaf(t0, r0, a0); a1 = fmaf(t0, r1, a1); a2 = fmaf(t0, r2, a2);
+        a3 = fmaf(t1, r1, a3); a4 = fmaf(t1, r2, a4); a5 = fmaf(t2, r2, a5);
+    }
+    (void)L2;
+    P[0] = fmaf(ws, a0, P[0]); P[1] = fmaf(ws, a1, P[1]); P[2] = fmaf(ws, a2, P[2]);
+    P[3] = fmaf(ws, a3, P[3]); P[4] = fmaf(ws, a4, P[4]); P[5] = fmaf(ws, a5, P[5]);
+}
+
+// the exact plate (closed form) of this lane's receiver over the window
+// without o = 0 (that term is always voted exactly in the main loop)
+template <bool BALL>
+__device__ __forceinline__ void plate_exact_sum(const SurVoteArgs& a, const float4* tbl, int x, int y, int z,
+                                                float* E) {
+    const FastArgs& f = a.f;
+    const int hw = f.hw, W = 2 * hw + 1;
+    for (int k = 0; k < 7; ++k) E[k] = 0.0f;
+    const float4 Z4 = make_float4(0, 0, 0, 0);
+    for (int oz = -hw; oz <= hw; ++oz) {
+        const int vz = z + oz;
+        if ((unsigned)vz >= (unsigned)f.s0) continue;
+        for (int oy = -hw; oy <= hw; ++oy) {
+            const int vy = y + oy;
+            if ((unsigned)vy >= (unsigned)f.s1) continue;
+            for (int ox = -hw; ox <= hw; ++ox) {
+                const int vx = x + ox;
+                const bool in = (unsigned)vx < (unsigned)f.s2;
+                const float4 B = in ? __ldg(f.B + (size_t(vz) * f.s1 + vy) * f.s2 + vx) : Z4;
+                const int L2 = ox * ox + oy * oy + oz * oz;
+                if (BALL) {   // the exact ball, every offset
+                    const float lb = in ? __ldg(f.C + (size_t(vz) * f.s1 + vy) * f.s2 + vx) : 0.0f;
+                    const float4* bt = reinterpret_cast<const float4*>(
+                        a.ball_exact + 8 * (size_t((oz + hw) * W + (oy + hw)) * W + (ox + hw)));
+                    const float4 b0 = __ldg(bt), b1 = __ldg(bt + 1);
+                    E[0] = fmaf(lb, b0.x, E[0]); E[1] = fmaf(lb, b0.y, E[1]); E[2] = fmaf(lb, b0.z, E[2]);
+                    E[3] = fmaf(lb, b0.w, E[3]); E[4] = fmaf(lb, b1.x, E[4]); E[5] = fmaf(lb, b1.y, E[5]);
+                }
+                if (L2 == 0) continue;
+                const float4 ta = tbl[2 * L2], tb = tbl[2 * L2 + 1];
+                vote_pair<false, true, false>(Z4, B, 0.0f, 0.0f, fmaf(B.x, float(ox), B.y * float(oy)), float(ox),
+                                              float(oy), float(oz), ta, tb, E);
+            }
+        }
+    }
+}
+
+template <int MODE, bool STICK, bool BALL>
+__global__ void __launch_bounds__(128) k_vote3_sur(SurVoteArgs a) {
+    extern __shared__ __align__(16) float4 sm4[];
+    const FastArgs& f = a.f;
+    const int hw = f.hw;
+    const int nt = 3 * hw * hw + 1;
+    float4* tbl = sm4;                                               // 2 nt float4
+    uint2* frag = reinterpret_cast<uint2*>(tbl + 2 * nt);            // SUR_NFRAG * 32
+    float* bias = reinterpret_cast<float*>(frag + SUR_NFRAG * 32);   // SUR_NBIAS
+    float* sacc = bias + SUR_NBIAS;                                  // 4 warps x 32 x 8
+    __shared__ int s_fail;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int L2 = tid; L2 < nt; L2 += 128) {
+        float4 ea, eb;
+        radial_entry(L2, f.sig1, f.sig2, ea, eb);
+        tbl[2 * L2] = ea;
+        tbl[2 * L2 + 1] = eb;
+    }
+    if (MODE == PLATE_SURROGATE) {
+        for (int e = tid; e < SUR_NFRAG * 32; e += 128) frag[e] = a.frag[e];
+        for (int e = tid; e < SUR_NBIAS; e += 128) bias[e] = a.bias[e];
+    }
+    if (tid == 0) s_fail = 0;
+    __syncthreads();
+
+    const int x = blockIdx.x * 32 + lane, y = blockIdx.y * 4 + warp, z = blockIdx.z;
+    const bool yin = y < f.s1;
+    const int g = lane >> 2, t = lane & 3;
+    const float4 Z4 = make_float4(0, 0, 0, 0);
+    float tot[6], cmp[6];
+    for (int k = 0; k < 6; ++k) { tot[k] = 0.0f; cmp[k] = 0.0f; }
+    float pl[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
+    float bs[6] = {0, 0, 0, 0, 0, 0};   // the network's ball (PLATE_SURROGATE), judged with the plate
+    const int W = 2 * hw + 1;
+    for (int oz = -hw; oz <= hw; ++oz) {
+        const int vz = z + oz;
+        if ((unsigned)vz >= (unsigned)f.s0) continue;
+        float P[7] = {0, 0, 0, 0, 0, 0, 0};
+        for (int oy = -hw; oy <= hw; ++oy) {
+            const int vy = y + oy;
+            if (!yin || (unsigned)vy >= (unsigned)f.s1) continue;   // warp-uniform
+            const size_t row = (size_t(vz) * f.s1 + vy) * f.s2;
+            for (int ox = -hw; ox <= hw; ++ox) {
+                const int vx = x + ox;
+                const bool in = (unsigned)vx < (unsigned)f.s2;
+                const float4 A = (STICK && in) ? __ldg(f.A + row + vx) : Z4;
+                const float4 B = in ? __ldg(f.B + row + vx) : Z4;
+                const int L2 = ox * ox + oy * oy + oz * oz;
+                const float4 ta = tbl[2 * L2], tb = tbl[2 * L2 + 1];
+                const float oxf = float(ox), oyf = float(oy), ozf = float(oz);
+                if (STICK)
+                    vote_pair<true, false, false>(A, Z4, 0.0f, fmaf(A.x, oxf, A.y * oyf), 0.0f, oxf, oyf, ozf, ta, tb, P);
+                if (BALL) {
+                    const float lb = in ? __ldg(f.C + row + vx) : 0.0f;
+                    const float4* bt = reinterpret_cast<const float4*>(
+                        a.ball_tab + 8 * (size_t((oz + hw) * W + (oy + hw)) * W + (ox + hw)));
+                    const float4 b0 = __ldg(bt), b1 = __ldg(bt + 1);
+                    float* D = MODE == PLATE_SURROGATE ? bs : P;
+                    D[0] = fmaf(lb, b0.x, D[0]); D[1] = fmaf(lb, b0.y, D[1]); D[2] = fmaf(lb, b0.z, D[2]);
+                    D[3] = fmaf(lb, b0.w, D[3]); D[4] = fmaf(lb, b1.x, D[4]); D[5] = fmaf(lb, b1.y, D[5]);
+                }
+                if (MODE == PLATE_CLOSED || L2 == 0) {
+                    vote_pair<false, true, false>(Z4, B, 0.0f, 0.0f, fmaf(B.x, oxf, B.y * oyf), oxf, oyf, ozf, ta, tb, P);
+                } else if (MODE == PLATE_PLAIN64) {
+                    plate_plain64(B, oxf, oyf, ozf, ta, float(L2), P);
+                } else {
+                    // network input of row r (pair of lane r): (o / |o|, n_r, 1, 0); this lane holds
+                    // columns 2t, 2t + 1 of rows g, g + 8 of each 16-row tile
+                    const float il = rsqrtf(float(L2));
+                    const float ins[4] = {oxf * il, oyf * il, ozf * il, 0.0f};
+                    const float c1 = ta.x;
+#pragma unroll 1
+                    for (int T = 0; T < 2; ++T) {
+                        const int r0 = 16 * T + g, r1 = r0 + 8;
+                        const float n0x = __shfl_sync(0xffffffffu, B.x, r0), n0y = __shfl_sync(0xffffffffu, B.y, r0);
+                        const float n0z = __shfl_sync(0xffffffffu, B.z, r0), s0w = __shfl_sync(0xffffffffu, B.w, r0);
+                        const float n1x = __shfl_sync(0xffffffffu, B.x, r1), n1y = __shfl_sync(0xffffffffu, B.y, r1);
+                        const float n1z = __shfl_sync(0xffffffffu, B.z, r1), s1w = __shfl_sync(0xffffffffu, B.w, r1);
+                        float lo0, hi0, lo1, hi1;
+                        if (t == 0) { lo0 = ins[0]; hi0 = ins[1]; lo1 = ins[0]; hi1 = ins[1]; }
+                        else if (t == 1) { lo0 = ins[2]; hi0 = n0x; lo1 = ins[2]; hi1 = n1x; }
+                        else if (t == 2) { lo0 = n0y; hi0 = n0z; lo1 = n1y; hi1 = n1z; }
+                        else { lo0 = 1.0f; hi0 = 0.0f; lo1 = 1.0f; hi1 = 0.0f; }
+                        const uint32_t fin[4] = {pack_bf16x2(lo0, hi0), pack_bf16x2(lo1, hi1), 0u, 0u};
+                        float out[4];
+                        sur_mlp16(frag, bias, fin, out);
+                        const float w0 = s0w * c1, w1 = s1w * c1;
+                        float* acc = T == 0 ? pl[0] : pl[1];
+                        acc[0] = fmaf(w0, out[0], acc[0]); acc[1] = fmaf(w0, out[1], acc[1]);
+                        acc[2] = fmaf(w1, out[2], acc[2]); acc[3] = fmaf(w1, out[3], acc[3]);
+                    }
+                }
+            }
+        }
+        kahan_add(tot[0], cmp[0], P[0] + P[6]);
+        kahan_add(tot[1], cmp[1], P[1]);
+        kahan_add(tot[2], cmp[2], P[2]);
+        kahan_add(tot[3], cmp[3], P[3] + P[6]);
+        kahan_add(tot[4], cmp[4], P[4]);
+        kahan_add(tot[5], cmp[5], P[5] + P[6]);
+    }
+    float plate[6] = {0, 0, 0, 0, 0, 0};
+    if (MODE == PLATE_SURROGATE) {
+        float* my = sacc + warp * 32 * 8;
+#pragma unroll
+        for (int T = 0; T < 2; ++T) {
+            my[(16 * T + g) * 8 + 2 * t] = pl[T][0];
+            my[(16 * T + g) * 8 + 2 * t + 1] = pl[T][1];
+            my[(16 * T + g + 8) * 8 + 2 * t] = pl[T][2];
+            my[(16 * T + g + 8) * 8 + 2 * t + 1] = pl[T][3];
+        }
+        __syncwarp();
+        for (int k = 0; k < 6; ++k) plate[k] = my[lane * 8 + k] + bs[k];
+        // judge: the first warp's receivers against the exact plate (and ball)
+        const bool mine = x < f.s2 && yin;
+        if (warp == 0) {
+            float E[7];
+            plate_exact_sum<BALL>(a, tbl, x, y, z, E);
+            const float e6[6] = {E[0] + E[6], E[1], E[2], E[3] + E[6], E[4], E[5] + E[6]};
+            float dn = 0.0f, tn = 0.0f;
+            for (int k = 0; k < 6; ++k) {
+                const float wgt = (k == 0 || k == 3 || k == 5) ? 1.0f : 2.0f;
+                const float d = plate[k] - e6[k], tt = tot[k] + e6[k];
+                dn = fmaf(wgt * d, d, dn);
+                tn = fmaf(wgt * tt, tt, tn);
+            }
+            const bool bad = mine && !(dn <= a.tol * a.tol * tn);
+            if (__any_sync(0xffffffffu, bad) && lane == 0) s_fail = 1;
+        }
+        __syncthreads();
+        if (s_fail) {
+            float E[7];
+            plate_exact_sum<BALL>(a, tbl, x, y, z, E);
+            plate[0] = E[0] + E[6]; plate[1] = E[1]; plate[2] = E[2];
+            plate[3] = E[3] + E[6]; plate[4] = E[4]; plate[5] = E[5] + E[6];
+        }
+        if (tid == 0 && a.stats) {
+            atomicAdd(a.stats, 1u);
+            if (s_fail) atomicAdd(a.stats + 1, 1u);
+        }
+    }
+    if (x >= f.s2 || !yin) return;
+    const size_t plane = size_t(f.s1) * f.s2, n = size_t(f.s0) * plane;
+    float m6[6];
+    for (int k = 0; k < 6; ++k) m6[k] = tot[k] + plate[k];
+    write_receiver(f, size_t(z) * plane + size_t(y) * f.s2 + x, n, m6);
+}
+
+// the per-offset ball table: lambda0-unit ball vote at each offset of the window
+template <int MODE>
+__global__ void k_ball_table(int hw, float sig1, float sig2, float inv_sig, const float* __restrict__ Fnet,
+                             float* __restrict__ tab) {
+    const int W = 2 * hw + 1;
+    const int n = W * W * W;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int ox = i % W - hw, oy = (i / W) % W - hw, oz = i / (W * W) - hw;
+        const int L2 = ox * ox + oy * oy + oz * oz;
+        float4 ea, eb;
+        radial_entry(L2, sig1, sig2, ea, eb);
+        float F[6] = {0, 0, 0, 0, 0, 0};
+        if (MODE == PLATE_CLOSED || L2 == 0) {
+            // (c1/3 + ct [o != 0]/15) I + (2 ct g / 15) o o^T: eb.z, eb.w
+            const float o[3] = {float(ox), float(oy), float(oz)};
+            F[0] = eb.z + eb.w * o[0] * o[0]; F[1] = eb.w * o[0] * o[1]; F[2] = eb.w * o[0] * o[2];
+            F[3] = eb.z + eb.w * o[1] * o[1]; F[4] = eb.w * o[1] * o[2]; F[5] = eb.z + eb.w * o[2] * o[2];
+        } else if (MODE == PLATE_PLAIN64) {
+            const float il = rsqrtf(float(L2));
+            const float d[3] = {ox * il, oy * il, oz * il};
+            const float c1 = ea.x, c2 = c1 + ea.y * float(L2);
+            for (int ia = 0; ia < 8; ++ia)
+                for (int ib = 0; ib < 8; ++ib) {
+                    const float ct = c_gl8x_v[ia], st = sqrtf(1.0f - ct * ct);
+                    float sp, cp;
+                    sincospif(float(ib) / 4.0f, &sp, &cp);
+                    const float q[3] = {st * cp, st * sp, ct};
+                    const float qd = q[0] * d[0] + q[1] * d[1] + q[2] * d[2];
+                    const float eta = c_gl8w_v[ia] * (1.0f / 16.0f) * (c1 * (1.0f - qd * qd) + c2 * qd * qd);
+                    const float r[3] = {q[0] - 2 * qd * d[0], q[1] - 2 * qd * d[1], q[2] - 2 * qd * d[2]};
+                    F[0] += eta * r[0] * r[0]; F[1] += eta * r[0] * r[1]; F[2] += eta * r[0] * r[2];
+                    F[3] += eta * r[1] * r[1]; F[4] += eta * r[1] * r[2]; F[5] += eta * r[2] * r[2];
+                }
+        } else {
+            for (int k = 0; k < 6; ++k) F[k] = ea.x * Fnet[size_t(i) * 8 + k];
+        }
+        for (int k = 0; k < 6; ++k) tab[size_t(i) * 8 + k] = F[k];
+        tab[size_t(i) * 8 + 6] = 0.0f;
+        tab[size_t(i) * 8 + 7] = 0.0f;
+    }
+}
+
+template <int MODE>
+static int launch_sur(const SurVoteArgs& a, bool S, bool B, dim3 grid, size_t smem, cudaStream_t st) {
+    const void* fn;
+    if (S && B) fn = (const void*)k_vote3_sur<MODE, true, true>;
+    else if (S) fn = (const void*)k_vote3_sur<MODE, true, false>;
+    else if (B) fn = (const void*)k_vote3_sur<MODE, false, true>;
+    else fn = (const void*)k_vote3_sur<MODE, false, false>;
+    TVGB_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    SurVoteArgs arg = a;
+    void* args[] = {&arg};
+    {
+        KernelTimer kt_(MODE == PLATE_SURROGATE ? "k_vote3_sur" : (MODE == PLATE_CLOSED ? "k_vote3_sur_closed"
+                                                                                       : "k_vote3_sur_plain64"), st);
+        TVGB_CUDA(cudaLaunchKernel(fn, grid, dim3(128), args, smem, st));
+        kt_.stop();
+    }
+    TVGB_LAUNCHED();
+    return TVGB_OK;
+}
+
+static int sur_constants() {
+    static std::mutex mu;
+    static bool done[64] = {};
+    int dev = 0;
+    TVGB_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(mu);
+    if (dev >= 0 && dev < 64 && done[dev]) return TVGB_OK;
+    float cs[64], sn[64];
+    for (int i = 0; i < 64; ++i) {
+        cs[i] = float(std::cos(3.14159265358979323846 * i / 64.0));
+        sn[i] = float(std::sin(3.14159265358979323846 * i / 64.0));
+    }
+    TVGB_CUDA(cudaMemcpyToSymbol(c_cs64, cs, sizeof(cs)));
+    TVGB_CUDA(cudaMemcpyToSymbol(c_sn64, sn, sizeof(sn)));
+    if (dev >= 0 && dev < 64) done[dev] = true;
+    return TVGB_OK;
+}
+
+}  // namespace tvgb
+
+extern "C" int tvgb_vote3_surrogate(const float* in, int in_layout, unsigned s0, unsigned s1, unsigned s2,
+                                    const tvgb_vote3_params* p, const float* net_params, int plate_mode, float tol,
+                                    float* out, int out_layout, float* evals3, float* evecs, int evec_format,
+                                    unsigned long long* stats, void* stream) {
+    using namespace tvgb;
+    TVGB_TRY(check_params(p, "tvgb_vote3_surrogate"));
+    TVGB_CHECK_ARG(!p->is_atv && (p->power <= 1) && p->sigma2 == 0.0f && p->sigma1 > 0.0f,
+                   "tvgb_vote3_surrogate: TK with power 1 and sigma2 = 0 only (the surrogate's training domain)");
+    TVGB_CHECK_ARG(plate_mode >= 0 && plate_mode <= 2, "tvgb_vote3_surrogate: plate_mode must be 0, 1 or 2");
+    TVGB_CHECK_ARG(plate_mode != 0 || net_params, "tvgb_vote3_surrogate: plate_mode 0 needs the network parameters");
+    TVGB_CHECK_ARG(tol >= 0.0f, "tvgb_vote3_surrogate: tol must be >= 0");
+    TVGB_CHECK_ARG(in_layout == TVGB_LAYOUT_MAT3 || in_layout == TVGB_LAYOUT_SYM6 || in_layout == TVGB_LAYOUT_SYM6_PLANES,
+                   "tvgb_vote3_surrogate: in_layout must be 9, 6 or 60");
+    TVGB_CHECK_ARG(out_layout == TVGB_LAYOUT_MAT3 || out_layout == TVGB_LAYOUT_SYM6 || out_layout == TVGB_LAYOUT_SYM6_PLANES,
+                   "tvgb_vote3_surrogate: out_layout must be 9, 6 or 60");
+    TVGB_CHECK_ARG(evec_format >= 0 && evec_format <= 2, "tvgb_vote3_surrogate: evec_format must be 0, 1 or 2");
+    const size_t n = size_t(s0) * s1 * s2;
+    if (stats) { stats[0] = 0; stats[1] = 0; }
+    if (n == 0) return TVGB_OK;
+    TVGB_CHECK_ARG(in, "tvgb_vote3_surrogate: input is NULL");
+    cudaStream_t st = as_stream(stream);
+    TVGB_TRY(sur_constants());
+    const size_t nin = in_layout == TVGB_LAYOUT_MAT3 ? 9 : 6, nout = out_layout == TVGB_LAYOUT_MAT3 ? 9 : 6;
+    const size_t nv = evec_format == 1 ? 9 : (evec_format == 2 ? 6 : 0);
+    DevArray din, dout, dev_, dvec;
+    TVGB_TRY(din.in(in, n * nin * 4, st));
+    TVGB_TRY(dout.out(out, n * nout * 4, st));
+    TVGB_TRY(dev_.out(evals3, n * 12, st));
+    TVGB_TRY(dvec.out(nv ? evecs : nullptr, n * nv * 4, st));
+
+    const unsigned w = p->w ? p->w : auto_window(p->sigma1, p->sigma2);
+    const int hw = int(w / 2), W = int(w);
+    const bool S = p->stick != 0, P = p->plate != 0, B = p->ball != 0;
+    Scratch sA, sB, sC, stab, stabx, snet, sX, sY, sst;
+    PrepOut po{};
+    TVGB_TRY(sA.alloc(n * 16, st)); po.A = sA.get<float4>();
+    TVGB_TRY(sB.alloc(n * 16, st)); po.B = sB.get<float4>();
+    if (B) { TVGB_TRY(sC.alloc(n * 4, st)); po.C = sC.get<float>(); }
+    const float sn = S ? 1.0f / sticknorm3_f(p->sigma1, p->sigma2, 1) : 1.0f;
+    TVGB_TRY(launch_prep(din.get<float>(), in_layout, n, po, sn, p->parity, st));
+    if (!P) TVGB_CUDA(cudaMemsetAsync(po.B, 0, n * 16, st));   // no plate: zero plate records
+
+    SurVoteArgs a{};
+    FastArgs& fa = a.f;
+    fa.A = po.A; fa.B = po.B; fa.C = po.C;
+    fa.s0 = int(s0); fa.s1 = int(s1); fa.s2 = int(s2); fa.hw = hw;
+    fa.sig1 = p->sigma1; fa.sig2 = p->sigma2;
+    fa.out = dout.get<float>(); fa.out_layout = out_layout; fa.evals = dev_.get<float>(); fa.evecs = dvec.get<float>();
+    fa.evec_fmt = nv ? evec_format : 0;
+    fa.precise_eig = p->parity ? 0 : 1;
+    a.inv_sig = 1.0f / p->sigma1;
+    a.tol = tol;
+    if (plate_mode == PLATE_SURROGATE) {
+        TVGB_TRY(snet.alloc(SUR_NFRAG * 32 * sizeof(uint2) + SUR_NBIAS * 4, st));
+        a.frag = snet.get<uint2>();
+        a.bias = reinterpret_cast<float*>(snet.get<uint2>() + SUR_NFRAG * 32);
+        TVGB_TRY(sur_upload(net_params, const_cast<uint2*>(a.frag), const_cast<float*>(a.bias), st));
+    }
+    if (B) {
+        const size_t nt3 = size_t(W) * W * W;
+        TVGB_TRY(stab.alloc(nt3 * 32, st));
+        const float* Fnet = nullptr;
+        if (plate_mode == PLATE_SURROGATE) {
+            std::vector<float> X(nt3 * 8, 0.0f);
+            for (size_t i = 0; i < nt3; ++i) {
+                const int ox = int(i % W) - hw, oy = int((i / W) % W) - hw, oz = int(i / (size_t(W) * W)) - hw;
+                const int L2 = ox * ox + oy * oy + oz * oz;
+                const float il = L2 ? 1.0f / std::sqrt(float(L2)) : 0.0f;   // o = 0 is tabulated exactly
+                X[i * 8 + 0] = ox * il; X[i * 8 + 1] = oy * il; X[i * 8 + 2] = oz * il;
+                X[i * 8 + 5] = 1.0f;   // any unit normal: the ball does not depend on it
+            }
+            TVGB_TRY(sX.alloc(nt3 * 32, st));
+            TVGB_TRY(sY.alloc(nt3 * 32, st));
+            TVGB_CUDA(cudaMemcpyAsync(sX.p, X.data(), nt3 * 32, cudaMemcpyHostToDevice, st));
+            TVGB_TRY(sur_eval_device(a.frag, a.bias, sX.get<float>(), nt3, sY.get<float>(), st));
+            TVGB_CUDA(cudaStreamSynchronize(st));   // X leaves scope
+            Fnet = sY.get<float>();
+        }
+        const unsigned gb = unsigned(std::min<size_t>((nt3 + 255) / 256, 4096));
+        if (plate_mode == PLATE_SURROGATE) {
+            TVGB_TRY(stabx.alloc(nt3 * 32, st));
+            k_ball_table<PLATE_CLOSED><<<gb, 256, 0, st>>>(hw, p->sigma1, p->sigma2, a.inv_sig, nullptr,
+                                                           stabx.get<float>());
+            TVGB_LAUNCHED();
+            a.ball_exact = stabx.get<float>();
+        }
+        if (plate_mode == PLATE_SURROGATE)
+            k_ball_table<PLATE_SURROGATE><<<gb, 256, 0, st>>>(hw, p->sigma1, p->sigma2, a.inv_sig, Fnet, stab.get<float>());
+        else if (plate_mode == PLATE_CLOSED)
+            k_ball_table<PLATE_CLOSED><<<gb, 256, 0, st>>>(hw, p->sigma1, p->sigma2, a.inv_sig, Fnet, stab.get<float>());
+        else
+            k_ball_table<PLATE_PLAIN64><<<gb, 256, 0, st>>>(hw, p->sigma1, p->sigma2, a.inv_sig, Fnet, stab.get<float>());
+        TVGB_LAUNCHED();
+        a.ball_tab = stab.get<float>();
+    }
+    TVGB_TRY(sst.alloc(16, st));
+    TVGB_CUDA(cudaMemsetAsync(sst.p, 0, 16, st));
+    a.stats = sst.get<unsigned>();
+    const int nt = 3 * hw * hw + 1;
+    const size_t smem = size_t(2) * nt * 16 + SUR_NFRAG * 32 * sizeof(uint2) + SUR_NBIAS * 4 + 4 * 32 * 8 * 4;
+    TVGB_CHECK_ARG(smem <= 200 * 1024, "tvgb_vote3_surrogate: window w = %u too large", w);
+    dim3 grid(ceil_div(s2, 32u), ceil_div(s1, 4u), s0);
+    if (plate_mode == PLATE_SURROGATE) TVGB_TRY(launch_sur<PLATE_SURROGATE>(a, S, B, grid, smem, st));
+    else if (plate_mode == PLATE_CLOSED) TVGB_TRY(launch_sur<PLATE_CLOSED>(a, S, B, grid, smem, st));
+    else TVGB_TRY(launch_sur<PLATE_PLAIN64>(a, S, B, grid, smem, st));
+    unsigned hst[2] = {0, 0};
+    TVGB_CUDA(cudaMemcpyAsync(hst, sst.p, 8, cudaMemcpyDeviceToHost, st));
+    TVGB_TRY(dout.finish());
+    TVGB_TRY(dev_.finish());
+    TVGB_TRY(dvec.finish());
+    TVGB_CUDA(cudaStreamSynchronize(st));
+    if (stats) { stats[0] = hst[0]; stats[1] = hst[1]; }
+    return TVGB_OK;
+}
