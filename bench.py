@@ -61,13 +61,15 @@ FLOPS_PER_PAIR_BALL = 18
 FP32_LANES_PER_SM = 128
 
 
-def pairs_count(dims, hw):
+def pairs_count(dims, hw, zrange=None):
     """Exact number of in-bounds (receiver, voter) pairs: product over axes of
-    sum_x #{o in [-hw, hw] : 0 <= x + o < s}."""
+    sum_x #{o in [-hw, hw] : 0 <= x + o < s}; zrange restricts the receivers'
+    first axis to [z0, z1) (a z-slab)."""
     p = 1
-    for s in dims:
+    for axis, s in enumerate(dims):
+        lo, hi = zrange if (axis == 0 and zrange) else (0, s)
         tot = 0
-        for x in range(s):
+        for x in range(lo, hi):
             tot += min(s - 1, x + hw) - max(0, x - hw) + 1
         p *= tot
     return p
@@ -295,9 +297,19 @@ def run_ours(args, rank, world, local_rank):
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     kw = dict(sigma_st=cfg["sigma_st"], sigma1=cfg["sigma"], w=cfg["w"], samples=cfg["samples"], st_mode="same",
               out_layout="planes", evecs="cartesian", ball=cfg["ball"])
+    strong = args.split == "slabs" and world > 1
+    if strong:
+        # strong scaling: one volume, each rank votes its z-slab (+ halos); no collective on the data path
+        from tiralib_gb300 import slabs
+        z0, z1 = slabs.partition(dims[0], world)[rank]
+        skw = dict(sigma_st=cfg["sigma_st"], sigma1=cfg["sigma"], w=cfg["w"], samples=cfg["samples"],
+                   ball=cfg["ball"])
 
     def step():
-        tv.pipeline3(vol_d, outputs=(out_d, ev_d, vec_d), **kw)
+        if strong:
+            slabs.pipeline3_slab(vol_d, z0, z1, **skw)
+        else:
+            tv.pipeline3(vol_d, outputs=(out_d, ev_d, vec_d), **kw)
 
     for _ in range(args.warmup):
         step()
@@ -341,7 +353,7 @@ def run_ours(args, rank, world, local_rank):
         tt = torch.tensor([t_local], device=dev)
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         t_max = float(tt.item())
-    value = world * args.steps * nvox / t_max
+    value = (1 if strong else world) * args.steps * nvox / t_max
 
     # ---- end to end through the C ABI with pinned host buffers
     out_h = torch.empty((6,) + dims).pin_memory()
@@ -350,7 +362,10 @@ def run_ours(args, rank, world, local_rank):
     vol_hn, out_hn, ev_hn, vec_hn = vol_h.numpy(), out_h.numpy(), ev_h.numpy(), vec_h.numpy()
 
     def step_e2e():
-        tv.pipeline3(vol_hn, outputs=(out_hn, ev_hn, vec_hn), **kw)
+        if strong:
+            slabs.pipeline3_slab(vol_hn, z0, z1, **skw)
+        else:
+            tv.pipeline3(vol_hn, outputs=(out_hn, ev_hn, vec_hn), **kw)
 
     step_e2e()
     if dist:
@@ -367,9 +382,13 @@ def run_ours(args, rank, world, local_rank):
         tt = torch.tensor([t_e2e], device=dev)
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         t_e2e = float(tt.item())
-    e2e_value = world * args.steps * nvox / t_e2e
+    e2e_value = (1 if strong else world) * args.steps * nvox / t_e2e
     h2d = vol_np.nbytes
     d2h = out_h.numel() * 4 + ev_h.numel() * 4 + vec_h.numel() * 4
+    if strong:   # this rank's share: its input planes with halos, its output planes
+        (il, ih), _ = slabs.halo_ranges(dims[0], z0, z1, cfg["sigma_st"], cfg["sigma"], 0.0, cfg["w"])
+        h2d = vol_np[il:ih].nbytes
+        d2h = d2h * (z1 - z0) // dims[0]
 
     # ---- roofline of the dominant kernel
     props = torch.cuda.get_device_properties(dev)
@@ -380,7 +399,8 @@ def run_ours(args, rank, world, local_rank):
     roofline = None
     if nl:
         avg_s = tot_ms / nl / 1e3
-        flops = pairs_count(dims, cfg["w"] // 2) * (FLOPS_PER_PAIR + (FLOPS_PER_PAIR_BALL if cfg["ball"] else 0))
+        flops = pairs_count(dims, cfg["w"] // 2, (z0, z1) if strong else None) * \
+            (FLOPS_PER_PAIR + (FLOPS_PER_PAIR_BALL if cfg["ball"] else 0))
         achieved = flops / avg_s / 1e12
         roofline = {"bound": "fp32", "kernel": "k_vote3_fast", "achieved": achieved, "peak": peak,
                     "unit": "TFLOP/s", "frac": achieved / peak,
@@ -402,7 +422,9 @@ def run_ours(args, rank, world, local_rank):
         line = {
             "metric": metric_for(cfg), "value": value, "unit": "voxels/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config_dict(cfg),
+            "scaling": "strong" if strong else "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": dict(config_dict(cfg), parallelism=(f"z-slabs x{world} (halo planes, no collective)" if strong
+                                                          else f"replicas x{world}")),
             "e2e": {"value": e2e_value, "unit": "voxels/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
             "kernels": {k: {"launches": v[0], "total_ms": v[1]} for k, v in prof.items()},
@@ -516,19 +538,18 @@ def run_c3(args, rank, world, local_rank):
         lib.tvgb_profile_enable(0)
         return float(np.sum(ts)) / 1e3, launches, parse_profile(buf.value.decode())
 
+    # precision on a 2^16 sample of the timed runs' own outputs (every chunk of the batch)
+    idx = torch.randperm(n, device=dev, generator=torch.Generator(device=dev).manual_seed(9))[: 1 << 16]
     with ClockSampler(gpu_index_for(local_rank)) as clk:
         t_precise, launches, prof = timed(True)
     clocks = clk.summary()
+    ev_p, vec_p = ev[idx].cpu().numpy(), vec[idx].cpu().numpy()
     t_parity, _, prof_par = timed(False)
+    ev_r, vec_r = ev[idx].cpu().numpy(), vec[idx].cpu().numpy()
     _, _, nref = tv.eig3(mats[: 1 << 20], precise=True)
-    # precision on a 2^16 sample of the same tensors
-    idx = torch.randperm(n, device=dev, generator=torch.Generator(device=dev).manual_seed(9))[: 1 << 16]
-    m_s = mats[idx].contiguous()
-    ev_p, vec_p, _ = tv.eig3(m_s, precise=True)
-    ev_r, vec_r, _ = tv.eig3(m_s, precise=False)
-    m_h = m_s.cpu().numpy()
-    err_precise = eigen_errors(m_h, ev_p.cpu().numpy(), vec_p.cpu().numpy())
-    err_parity = eigen_errors(m_h, ev_r.cpu().numpy(), vec_r.cpu().numpy())
+    m_h = mats[idx].cpu().numpy()
+    err_precise = eigen_errors(m_h, ev_p, vec_p)
+    err_parity = eigen_errors(m_h, ev_r, vec_r)
     # end to end with pinned host buffers
     mats_h = mats.cpu().pin_memory()
     ev_h = torch.empty((n, 3)).pin_memory()
@@ -541,15 +562,20 @@ def run_c3(args, rank, world, local_rank):
         tv.api.call("tvgb_eig3", tv.api._ptr(mn), 9, n, tv.api._ptr(evn), tv.api._ptr(vecn), 1, 1, None, None)
         e2e.append(time.perf_counter() - t0)
     peaks = measured_peaks()
+    # the precise call is k_eig3 (FP32 pass) + k_eig3_refine (FP64 queue) per chunk of 2^26 tensors:
+    # its roofline is the call's algorithmic bytes over the two kernels' time per call
     nl, tot = prof.get("k_eig3", (0, 0.0))
+    _, tot_r = prof.get("k_eig3_refine", (0, 0.0))
     bytes_per = 36 + 12 + 36
     roof = None
     if nl:
-        avg = tot / nl / 1e3
+        avg = (tot + tot_r) / args.steps / 1e3
         ach = n * bytes_per / avg / 1e9
-        roof = {"bound": "hbm", "kernel": "k_eig3 (precise)", "achieved": ach, "peak": peaks["hbm_gbs"],
-                "unit": "GB/s", "frac": ach / peaks["hbm_gbs"], "peak_source": peaks["source"],
-                "traffic": profiled_traffic("k_eig3", "c3"), "bytes_per_tensor": bytes_per, "avg_launch_ms": avg * 1e3}
+        roof = {"bound": "hbm", "kernel": "k_eig3 + k_eig3_refine (precise, per call)", "achieved": ach,
+                "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": ach / peaks["hbm_gbs"],
+                "peak_source": peaks["source"], "traffic": profiled_traffic("k_eig3", "c3"),
+                "bytes_per_tensor": bytes_per, "avg_call_kernel_ms": avg * 1e3,
+                "fp32_pass_ms": tot / args.steps, "fp64_pass_ms": tot_r / args.steps}
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         v, th, desc = cpu_eigen_sample()
@@ -782,6 +808,8 @@ def main():
     ap.add_argument("--config", choices=["c2", "c4", "c5", "c3", "c1"], default="c2",
                     help="c2: 3D pipeline, 256^3 (the headline); c4: the same at 384^3; c5: 512^3 tubes + sheets, "
                          "sigma 6, stick + plate + ball (capacity); c3: batched 3x3 eigen; c1: 2D pipeline")
+    ap.add_argument("--split", choices=["replicas", "slabs"], default="replicas",
+                    help="N > 1: independent replicas (weak scaling) or z-slabs of one volume (strong scaling)")
     ap.add_argument("--size", type=int, default=0, help="c2/c4/c5: volume edge (default 256/384/512); c3: log2 of "
                                                         "the tensor count (default 27); c1: image edge (default "
                                                         "512). Smaller sizes are for profiler captures")

@@ -442,6 +442,245 @@ __global__ void __launch_bounds__(VX * VY, TVGB_FAST_MINB) k_vote3_fast(FastArgs
     }
 }
 
+// ------------------------------------------------------------------ packed variant
+// The same arithmetic as k_vote3_fast with the two z-neighbour receivers
+// (j, j + 1) of a thread in the two lanes of Blackwell's packed FP32
+// instructions (FFMA2 / FMUL2 / FADD2): both see the same voter, so the
+// voter's components are broadcast and only the per-offset weights differ.
+// Those depend on |o|^2 = ox^2 + oy^2 + oz^2, so at each voter plane the CTA
+// builds a paired table indexed by ox^2 + oy^2 whose fields are already the
+// (j, j + 1) float2 pairs: a 128-bit load yields two packed operands.  One
+// packed instruction does two receivers' work, halving the FP32 issue slots
+// per pair.  Measured (256^3, sigma 4): 55 -> 35 instructions per pair,
+// issue active 77 % -> 49 %, but the FMA pipe, not issue, then bounds it
+// (a packed instruction holds the pipe twice as long): 420.7 ms against
+// 424.8 ms for k_vote3_fast.  With the ball term the packed kernel spills,
+// so ball votes keep k_vote3_fast.  Accumulation (plane partials into
+// per-voxel Kahan sums) is unchanged.
+#ifndef TVGB_PACKED
+#define TVGB_PACKED 1
+#endif
+#ifndef TVGB_PK_UNROLL
+#define TVGB_PK_UNROLL 2
+#endif
+constexpr int kPkUnroll = TVGB_PK_UNROLL;
+
+__device__ __forceinline__ float2 bc2(float x) { return make_float2(x, x); }
+
+// paired-table entry: X = (c1, ctg), Y = (-2g, A0), Z = (-A1, Bp), W = (ball I, ball oo^T), each a (j, j+1) pair
+template <bool STICK, bool PLATE, bool BALL>
+__device__ __forceinline__ void vote_pair_pk(const float4& A, const float4& B, float lb, float ub, float vb,
+                                             const float2& ox2, const float2& oy2, const float2& oz2, const float4& X,
+                                             const float4& Y, const float4& Z, const float4& W, float2 (&P)[7]) {
+    const float2 F2n = make_float2(Y.x, Y.y);
+    if (STICK) {
+        const float2 u = __ffma2_rn(bc2(A.z), oz2, bc2(ub));            // q . o
+        const float2 kn = __fmul2_rn(u, F2n);                             // -2 (q.o) / |o|^2
+        const float2 rx = __ffma2_rn(kn, ox2, bc2(A.x));
+        const float2 ry = __ffma2_rn(kn, oy2, bc2(A.y));
+        const float2 rz = __ffma2_rn(kn, oz2, bc2(A.z));
+        const float2 eta = __ffma2_rn(make_float2(X.z, X.w), __fmul2_rn(u, u), make_float2(X.x, X.y));
+        const float2 term = __fmul2_rn(bc2(A.w), eta);
+        const float2 t0 = __fmul2_rn(term, rx), t1 = __fmul2_rn(term, ry), t2 = __fmul2_rn(term, rz);
+        P[0] = __ffma2_rn(t0, rx, P[0]);
+        P[1] = __ffma2_rn(t0, ry, P[1]);
+        P[2] = __ffma2_rn(t0, rz, P[2]);
+        P[3] = __ffma2_rn(t1, ry, P[3]);
+        P[4] = __ffma2_rn(t1, rz, P[4]);
+        P[5] = __ffma2_rn(t2, rz, P[5]);
+    }
+    if (PLATE) {
+        const float2 v = __ffma2_rn(bc2(B.z), oz2, bc2(vb));            // n . o
+        const float2 kn = __fmul2_rn(v, F2n);
+        const float2 mx = __ffma2_rn(kn, ox2, bc2(B.x));                  // m = R n
+        const float2 my = __ffma2_rn(kn, oy2, bc2(B.y));
+        const float2 mz = __ffma2_rn(kn, oz2, bc2(B.z));
+        const float2 hx = __ffma2_rn(v, mx, ox2);                         // h = o + v m
+        const float2 hy = __ffma2_rn(v, my, oy2);
+        const float2 hz = __ffma2_rn(v, mz, oz2);
+        const float2 cA = __ffma2_rn(make_float2(Z.x, Z.y), __fmul2_rn(v, v), make_float2(Y.z, Y.w));
+        const float2 nsA = __fmul2_rn(bc2(-B.w), cA);                     // -sA
+        const float2 sB = __fmul2_rn(bc2(B.w), make_float2(Z.z, Z.w));
+        P[6] = __fadd2_rn(P[6], nsA);                                     // the identity term, negated
+        const float2 ax = __fmul2_rn(nsA, mx), ay = __fmul2_rn(nsA, my), az = __fmul2_rn(nsA, mz);
+        const float2 bx = __fmul2_rn(sB, hx), by = __fmul2_rn(sB, hy), bz = __fmul2_rn(sB, hz);
+        P[0] = __ffma2_rn(bx, hx, __ffma2_rn(ax, mx, P[0]));
+        P[1] = __ffma2_rn(bx, hy, __ffma2_rn(ax, my, P[1]));
+        P[2] = __ffma2_rn(bx, hz, __ffma2_rn(ax, mz, P[2]));
+        P[3] = __ffma2_rn(by, hy, __ffma2_rn(ay, my, P[3]));
+        P[4] = __ffma2_rn(by, hz, __ffma2_rn(ay, mz, P[4]));
+        P[5] = __ffma2_rn(bz, hz, __ffma2_rn(az, mz, P[5]));
+    }
+    if (BALL) {
+        P[6] = __ffma2_rn(bc2(-lb), make_float2(W.x, W.y), P[6]);
+        const float2 wb = __fmul2_rn(bc2(lb), make_float2(W.z, W.w));
+        const float2 wx = __fmul2_rn(wb, ox2), wy = __fmul2_rn(wb, oy2), wz = __fmul2_rn(wb, oz2);
+        P[0] = __ffma2_rn(wx, ox2, P[0]);
+        P[1] = __ffma2_rn(wx, oy2, P[1]);
+        P[2] = __ffma2_rn(wx, oz2, P[2]);
+        P[3] = __ffma2_rn(wy, oy2, P[3]);
+        P[4] = __ffma2_rn(wy, oz2, P[4]);
+        P[5] = __ffma2_rn(wz, oz2, P[5]);
+    }
+}
+
+// one voter row (fixed vz, oy) against the receiver pair of this paired table
+template <bool STICK, bool PLATE, bool BALL>
+__device__ __forceinline__ void vote_row_pk(const float4* __restrict__ rA, const float4* __restrict__ rB,
+                                            const float* __restrict__ rC, const float4* __restrict__ pt, int NQ,
+                                            const float2& oz2, float oyf, int L2y, int hw, float2 (&P)[7]) {
+    const float4 Z4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const float2 oy2 = bc2(oyf);
+    {   // ox = 0
+        const float4 A = STICK ? rA[0] : Z4, B = PLATE ? rB[0] : Z4;
+        const float lb = BALL ? rC[0] : 0.0f;
+        const float4* e = pt + NQ * L2y;
+        const float4 X = e[0], Y = e[1], Zt = e[2], W = BALL ? e[3] : Z4;
+        vote_pair_pk<STICK, PLATE, BALL>(A, B, lb, A.y * oyf, B.y * oyf, bc2(0.0f), oy2, oz2, X, Y, Zt, W, P);
+    }
+    float oxf = 1.0f;
+    int e2 = 1 + L2y;
+    int step = 3;                        // (ox + 1)^2 - ox^2 for ox = 1
+#pragma unroll kPkUnroll
+    for (int d = 1; d <= hw; ++d) {
+        const float4 Ap = STICK ? rA[d] : Z4, Am = STICK ? rA[-d] : Z4;
+        const float4 Bp = PLATE ? rB[d] : Z4, Bm = PLATE ? rB[-d] : Z4;
+        const float lp = BALL ? rC[d] : 0.0f, lm = BALL ? rC[-d] : 0.0f;
+        const float4* e = pt + NQ * e2;
+        const float4 X = e[0], Y = e[1], Zt = e[2], W = BALL ? e[3] : Z4;
+        const float2 oxp = bc2(oxf), oxm = bc2(-oxf);
+        vote_pair_pk<STICK, PLATE, BALL>(Ap, Bp, lp, fmaf(Ap.x, oxf, Ap.y * oyf), fmaf(Bp.x, oxf, Bp.y * oyf), oxp, oy2,
+                                         oz2, X, Y, Zt, W, P);
+        vote_pair_pk<STICK, PLATE, BALL>(Am, Bm, lm, fmaf(-Am.x, oxf, Am.y * oyf), fmaf(-Bm.x, oxf, Bm.y * oyf), oxm,
+                                         oy2, oz2, X, Y, Zt, W, P);
+        e2 += step;
+        step += 2;
+        oxf += 1.0f;
+    }
+}
+
+template <bool STICK, bool PLATE, bool BALL>
+__global__ void __launch_bounds__(VX * VY, TVGB_FAST_MINB) k_vote3_pk(FastArgs a) {
+    constexpr int R = 4;
+    constexpr int NQ = BALL ? 4 : 3;         // float4 per paired-table entry
+    extern __shared__ __align__(16) float4 smem[];
+    const int hw = a.hw;
+    const int nt = 3 * hw * hw + 1;          // radial table entries
+    const int ne = 2 * hw * hw + 1;          // paired-table entries (ox^2 + oy^2)
+    const int SW = VX + 2 * hw;
+    const int SR = VY + a.rows - 1;
+    float4* tbl = smem;                      // 2 nt
+    float4* ptab = tbl + 2 * nt;             // 2 pairs x ne x NQ
+    float4* sA = ptab + 2 * ne * NQ;
+    float4* sB = sA + (STICK ? SR * SW : 0);
+    float* sC = reinterpret_cast<float*>(sB + (PLATE ? SR * SW : 0));
+    const int tid = threadIdx.y * VX + threadIdx.x;
+    const int nthr = VX * VY;
+    for (int L2 = tid; L2 < nt; L2 += nthr) {
+        float4 ea, eb;
+        radial_entry(L2, a.sig1, a.sig2, ea, eb);
+        tbl[2 * L2] = ea;
+        tbl[2 * L2 + 1] = eb;
+    }
+    const int x0 = blockIdx.x * VX, y0 = blockIdx.y * VY, z0 = blockIdx.z * R;
+    const int s0 = a.s0, s1 = a.s1, s2 = a.s2;
+    const size_t plane = size_t(s1) * s2;
+    float tot[R][6], cmp[R][6];
+#pragma unroll
+    for (int j = 0; j < R; ++j)
+#pragma unroll
+        for (int k = 0; k < 6; ++k) { tot[j][k] = 0.0f; cmp[j][k] = 0.0f; }
+
+    const int vz_lo = max(0, z0 - hw), vz_hi = min(s0 - 1, z0 + R - 1 + hw);
+    for (int vz = vz_lo; vz <= vz_hi; ++vz) {
+        const int dzp = vz - z0;
+        float2 P[2][7];
+#pragma unroll
+        for (int p = 0; p < 2; ++p)
+#pragma unroll
+            for (int k = 0; k < 7; ++k) P[p][k] = make_float2(0.0f, 0.0f);
+        // receiver pair p = (2p, 2p + 1): oz = dzp - j; a pair with neither receiver in reach is skipped
+        bool pv[2];
+        float2 oz2[2];
+#pragma unroll
+        for (int p = 0; p < 2; ++p) {
+            const int oa = dzp - 2 * p, ob = oa - 1;
+            pv[p] = abs(oa) <= hw || abs(ob) <= hw;
+            oz2[p] = make_float2(float(oa), float(ob));
+        }
+        for (int oy0 = -hw; oy0 <= hw; oy0 += a.rows) {
+            const int oy1 = min(hw, oy0 + a.rows - 1);
+            const int nrows = VY + (oy1 - oy0);
+            __syncthreads();   // previous stage fully consumed (and table built)
+            if (oy0 == -hw) {  // this plane's paired table (zero weights for a receiver out of reach)
+                for (int i = tid; i < 2 * ne; i += nthr) {
+                    const int p = i / ne, e = i - p * ne;
+                    const int oa = dzp - 2 * p, ob = oa - 1;
+                    float4 ta = make_float4(0, 0, 0, 0), tba = ta, tb = ta, tbb = ta;
+                    if (abs(oa) <= hw) { ta = tbl[2 * (e + oa * oa)]; tba = tbl[2 * (e + oa * oa) + 1]; }
+                    if (abs(ob) <= hw) { tb = tbl[2 * (e + ob * ob)]; tbb = tbl[2 * (e + ob * ob) + 1]; }
+                    float4* q = ptab + (size_t(p) * ne + e) * NQ;
+                    // radial entry a = (c1, ct g, 2 g, A0), b = (A1, Bp, ball I, ball oo^T)
+                    q[0] = make_float4(ta.x, tb.x, ta.y, tb.y);
+                    q[1] = make_float4(-ta.z, -tb.z, ta.w, tb.w);
+                    q[2] = make_float4(-tba.x, -tbb.x, tba.y, tbb.y);
+                    if (BALL) q[3] = make_float4(tba.z, tbb.z, tba.w, tbb.w);
+                }
+            }
+            const int nst = nrows * SW;
+            for (int e = tid; e < nst; e += nthr) {
+                const int r = e / SW, c = e - r * SW;
+                const int gy = y0 + oy0 + r, gx = x0 - hw + c;
+                const bool in = (unsigned)gy < (unsigned)s1 && (unsigned)gx < (unsigned)s2;
+                const size_t gi = size_t(vz) * plane + size_t(gy) * s2 + gx;
+                if (STICK) sA[e] = in ? __ldg(a.A + gi) : make_float4(0, 0, 0, 0);
+                if (PLATE) sB[e] = in ? __ldg(a.B + gi) : make_float4(0, 0, 0, 0);
+                if (BALL) sC[e] = in ? __ldg(a.C + gi) : 0.0f;
+            }
+            __syncthreads();
+            for (int oy = oy0; oy <= oy1; ++oy) {
+                if ((unsigned)(y0 + int(threadIdx.y) + oy) >= (unsigned)s1) continue;   // warp-uniform
+                const int rr = threadIdx.y + (oy - oy0);
+                const int base = rr * SW + threadIdx.x + hw;
+#pragma unroll
+                for (int p = 0; p < 2; ++p)
+                    if (pv[p])
+                        vote_row_pk<STICK, PLATE, BALL>(sA + base, sB + base, sC + base, ptab + size_t(p) * ne * NQ,
+                                                        NQ, oz2[p], float(oy), oy * oy, hw, P[p]);
+            }
+        }
+#pragma unroll
+        for (int p = 0; p < 2; ++p) {
+            const float2 d6 = P[p][6];   // negated identity term
+            kahan_add(tot[2 * p][0], cmp[2 * p][0], P[p][0].x - d6.x);
+            kahan_add(tot[2 * p][1], cmp[2 * p][1], P[p][1].x);
+            kahan_add(tot[2 * p][2], cmp[2 * p][2], P[p][2].x);
+            kahan_add(tot[2 * p][3], cmp[2 * p][3], P[p][3].x - d6.x);
+            kahan_add(tot[2 * p][4], cmp[2 * p][4], P[p][4].x);
+            kahan_add(tot[2 * p][5], cmp[2 * p][5], P[p][5].x - d6.x);
+            kahan_add(tot[2 * p + 1][0], cmp[2 * p + 1][0], P[p][0].y - d6.y);
+            kahan_add(tot[2 * p + 1][1], cmp[2 * p + 1][1], P[p][1].y);
+            kahan_add(tot[2 * p + 1][2], cmp[2 * p + 1][2], P[p][2].y);
+            kahan_add(tot[2 * p + 1][3], cmp[2 * p + 1][3], P[p][3].y - d6.y);
+            kahan_add(tot[2 * p + 1][4], cmp[2 * p + 1][4], P[p][4].y);
+            kahan_add(tot[2 * p + 1][5], cmp[2 * p + 1][5], P[p][5].y - d6.y);
+        }
+    }
+
+    const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
+    if (x >= s2 || y >= s1) return;
+    const size_t n = size_t(s0) * plane;
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+        const int z = z0 + j;
+        if (z >= s0) break;
+        float m6[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) m6[k] = tot[j][k];
+        write_receiver(a, size_t(z) * plane + size_t(y) * s2 + x, n, m6);
+    }
+}
+
 // ------------------------------------------------------------------ generic kernel
 // One receiver per thread, straight gather with the reference's arithmetic;
 // handles any power, a literal samples-point plate when samples < power + 2
@@ -669,10 +908,47 @@ static size_t fast_smem(int hw, int rows, bool S, bool P, bool B) {
            (B ? size_t(SR) * SW * 4 : 0);
 }
 
+template <bool S, bool P, bool B>
+static int launch_pk_t(const FastArgs& a, size_t smem, cudaStream_t st) {
+    TVGB_CUDA(cudaFuncSetAttribute(k_vote3_pk<S, P, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    dim3 grid(ceil_div(a.s2, VX), ceil_div(a.s1, VY), ceil_div(a.s0, 4));
+    {
+        KernelTimer kt_("k_vote3_fast", st);
+        k_vote3_pk<S, P, B><<<grid, dim3(VX, VY), smem, st>>>(a);
+        kt_.stop();
+    }
+    TVGB_LAUNCHED();
+    return TVGB_OK;
+}
+
+static size_t pk_smem(int hw, int rows, bool S, bool P, bool B) {
+    const size_t ne = size_t(2) * hw * hw + 1;
+    return fast_smem(hw, rows, S, P, B) + 2 * ne * (B ? 4 : 3) * 16;
+}
+
 static int launch_fast(FastArgs a, bool S, bool P, bool B, cudaStream_t st) {
     // rows per stage: the largest count that keeps TVGB_FAST_MINB CTAs per SM
     const int w = 2 * a.hw + 1;
     const size_t budget = (TVGB_FAST_MINB >= 3 ? 72 : 100) * 1024;
+    if (TVGB_PACKED && FAST_R == 4 && !B) {
+        int rows = w;
+        while (rows > 1 && pk_smem(a.hw, rows, S, P, B) > budget) rows = (rows + 1) / 2;
+        const size_t smem = pk_smem(a.hw, rows, S, P, B);
+        if (smem <= 200 * 1024) {
+            a.rows = rows;
+            const int code = (S ? 4 : 0) | (P ? 2 : 0) | (B ? 1 : 0);
+            switch (code) {
+                case 4: return launch_pk_t<true, false, false>(a, smem, st);
+                case 2: return launch_pk_t<false, true, false>(a, smem, st);
+                case 6: return launch_pk_t<true, true, false>(a, smem, st);
+                case 7: return launch_pk_t<true, true, true>(a, smem, st);
+                case 5: return launch_pk_t<true, false, true>(a, smem, st);
+                case 3: return launch_pk_t<false, true, true>(a, smem, st);
+                case 1: return launch_pk_t<false, false, true>(a, smem, st);
+                default: return TVGB_OK;
+            }
+        }
+    }
     int rows = w;
     while (rows > 1 && fast_smem(a.hw, rows, S, P, B) > budget) rows = (rows + 1) / 2;
     if (fast_smem(a.hw, rows, S, P, B) > 200 * 1024) {
