@@ -276,6 +276,13 @@ int tvgb_surrogate_train(float* params, const float* X, const float* T, size_t n
 /* The network on the tensor cores: Y (n x 8 floats, 6 used) from X. */
 int tvgb_surrogate_eval(const float* params, const float* X, size_t n, float* Y, void* stream);
 
+/* The same network on the fifth-generation tensor cores (tcgen05.mma, the
+ * activations in tensor memory, 128 samples per tile).  gelu_mode 0: GELU in
+ * FP32 with the hardware tanh, as tvgb_surrogate_eval; 1: GELU in packed
+ * BF16 arithmetic (the arithmetic of the training forward pass and of the
+ * surrogate vote).  Returns TVGB_ERR_CUDA if a tensor-core wait timed out. */
+int tvgb_surrogate_eval_tc(const float* params, const float* X, size_t n, float* Y, int gelu_mode, void* stream);
+
 /* tvgb_vote3 (TK, power 1, sigma2 = 0) with the plate (and ball) vote by
  * plate_mode: 0 the network (judged per CTA of 32 x 4 receivers: if any of
  * its first 32 receivers' plate differs from the exact plate by more than

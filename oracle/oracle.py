@@ -379,7 +379,10 @@ def mlp_param_count():
 
 def mlp_loss_grad(params, X, T, quant=True):
     """FP64 loss and gradient of the surrogate MLP over a batch: X (B, 8)
-    inputs, T (B, 8) targets (first 6 used).  Returns (loss, grad, Y)."""
+    inputs, T (B, 8) targets (first 6 used).  quant: False (exact), True / 1
+    (BF16 weights and layer inputs, GELU exact then rounded) or 2 (as 1 with
+    the GELU in packed BF16 arithmetic, as the GPU trains and votes).
+    Returns (loss, grad, Y)."""
     P = np.ascontiguousarray(params, np.float64)
     X = np.ascontiguousarray(X, np.float64).reshape(-1, 8)
     T = np.ascontiguousarray(T, np.float64).reshape(-1, 8)

@@ -9,7 +9,12 @@
  *   W1[64][8] b1[64] W2[64][64] b2[64] W3[64][64] b3[64] W4[8][64] b4[8]
  * Quantised forward (quant != 0): weights and each layer's input rounded to
  * bfloat16 (round to nearest even of the float32 value), as the tensor-core
- * inference computes; the backward pass treats the rounding as identity. */
+ * inference computes; the backward pass treats the rounding as identity.
+ * quant == 1: GELU exact, then rounded to bfloat16 (the GPU's FP32 GELU);
+ * quant == 2: GELU in packed BF16 arithmetic as the GPU's training forward
+ * pass and its tcgen05 inference compute it (every product or fused
+ * multiply-add rounded to bfloat16 once, tanh exact then rounded; the
+ * hardware's tanh approximation may differ from that in the last bit). */
 #include <math.h>
 #include <stdint.h>
 #include <string.h>
@@ -37,6 +42,15 @@ static const double GELU_K = 0.7978845608028654;   /* sqrt(2 / pi) */
 static const double GELU_A = 0.044715;
 
 static double gelu(double z) { return 0.5 * z * (1.0 + tanh(GELU_K * (z + GELU_A * z * z * z))); }
+static double gelu_bf16(double z) {
+    const double zb = bf16r(z);
+    const double ka = bf16r((float)GELU_K * (float)GELU_A), k = bf16r(GELU_K);
+    const double u = bf16r(zb * bf16r(bf16r(zb * zb) * ka + k));
+    const double t = bf16r(tanh(u));
+    const double h = bf16r(zb * 0.5);
+    return bf16r(h * t + h);
+}
+static double act(double z, int quant) { return quant == 2 ? gelu_bf16(z) : (quant ? bf16r(gelu(z)) : gelu(z)); }
 static double gelu_d(double z) {
     const double t = tanh(GELU_K * (z + GELU_A * z * z * z));
     return 0.5 * (1.0 + t) + 0.5 * z * (1.0 - t * t) * GELU_K * (1.0 + 3.0 * GELU_A * z * z);
@@ -82,19 +96,19 @@ double or_mlp_loss_grad(const double* P, const double* X, const double* T, int B
             double a = b1[j];
             for (int k = 0; k < MLP_IN; ++k) a += W1q[j * MLP_IN + k] * h0[k];
             z1[j] = a;
-            h1[j] = quant ? bf16r(gelu(a)) : gelu(a);
+            h1[j] = act(a, quant);
         }
         for (int j = 0; j < MLP_H; ++j) {
             double a = b2[j];
             for (int k = 0; k < MLP_H; ++k) a += W2q[j * MLP_H + k] * h1[k];
             z2[j] = a;
-            h2[j] = quant ? bf16r(gelu(a)) : gelu(a);
+            h2[j] = act(a, quant);
         }
         for (int j = 0; j < MLP_H; ++j) {
             double a = b3[j];
             for (int k = 0; k < MLP_H; ++k) a += W3q[j * MLP_H + k] * h2[k];
             z3[j] = a;
-            h3[j] = quant ? bf16r(gelu(a)) : gelu(a);
+            h3[j] = act(a, quant);
         }
         double dy[MLP_OUT];
         for (int o = 0; o < MLP_OUT; ++o) {

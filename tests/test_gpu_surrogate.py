@@ -43,7 +43,8 @@ def test_training_gradient_matches_fp64_mlp(S):
     p[S.layout()[-1][1] + 6:] = 0.0
     X, T = S.samples(256, seed=9)
     g, loss = S.grad(p, X, T)
-    loss_ref, g_ref, _ = O.mlp_loss_grad(p.astype(np.float64), X, T, quant=True)
+    # quant 2: the forward pass with the packed-BF16 GELU the GPU trains with
+    loss_ref, g_ref, _ = O.mlp_loss_grad(p.astype(np.float64), X, T, quant=2)
     assert loss == pytest.approx(loss_ref, rel=1e-3)
     # FP32 accumulation and rare flips of a bf16 rounding against the FP64 oracle
     assert np.linalg.norm(g - g_ref) <= 2e-3 * np.linalg.norm(g_ref)
@@ -54,14 +55,38 @@ def test_training_gradient_matches_fp64_mlp(S):
 
 
 def test_tensor_core_inference_matches_fp64_forward(S):
-    rng = np.random.default_rng(3)
     p = S.init_params(7)
     X, T = S.samples(5000, seed=3)
-    Y = S.evaluate(p, X)
-    _, _, Yref = O.mlp_loss_grad(p.astype(np.float64), X, T, quant=True)
+    # warp-level mma.sync, FP32 GELU
+    Y = S.evaluate(p, X, engine="mma", gelu="fp32")
+    _, _, Yref = O.mlp_loss_grad(p.astype(np.float64), X, T, quant=1)
     err = np.abs(Y[:, :6] - Yref[:, :6])
     scale = np.abs(Yref[:, :6]).max()
     assert np.median(err) <= 2e-3 * scale and err.max() <= 3e-2 * scale
+    # tcgen05 with the FP32 GELU: the same products and roundings as mma.sync;
+    # only the FP32 summation order inside the tensor core may differ
+    Ytc = S.evaluate(p, X, engine="tcgen05", gelu="fp32")
+    assert np.abs(Ytc[:, :6] - Y[:, :6]).max() <= 1e-3 * scale
+    assert np.all(Ytc[:, 6:] == 0)
+    # tcgen05 with the packed-BF16 GELU against the oracle's emulation of it
+    Yb = S.evaluate(p, X, engine="tcgen05", gelu="bf16")
+    _, _, Yref2 = O.mlp_loss_grad(p.astype(np.float64), X, T, quant=2)
+    err = np.abs(Yb[:, :6] - Yref2[:, :6])
+    assert np.median(err) <= 2e-3 * scale and err.max() <= 3e-2 * scale
+
+
+def test_tcgen05_inference_ragged_sizes(S):
+    """Sample counts that are not multiples of the 128-row tile, and more
+    tiles than CTAs (each CTA loops over tiles)."""
+    p = S.init_params(5)
+    for n in (1, 127, 129, 1000, 200_003):
+        X, T = S.samples(n, seed=n)
+        Y = S.evaluate(p, X)
+        _, _, Yref = O.mlp_loss_grad(p.astype(np.float64), X[:4000], T[:4000], quant=2)
+        scale = np.abs(Yref[:, :6]).max()
+        err = np.abs(Y[:4000, :6] - Yref[:, :6])
+        assert np.isfinite(Y).all()
+        assert np.median(err) <= 2e-3 * scale and err.max() <= 3e-2 * scale, n
 
 
 def test_training_reduces_the_loss(S, trained):

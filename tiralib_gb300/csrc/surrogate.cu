@@ -16,6 +16,7 @@
 // with its (u, v) basis) or over an 8 x 8 sphere rule (ball), r = q - 2 (q.d) d.
 #include "tvgb_internal.cuh"
 #include "surrogate_mlp.cuh"
+#include "sur_tc.cuh"
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -53,6 +54,37 @@ void sur_make_fragments(const float* P, uint2* frag, float* bias) {
         bias[2 * SUR_H + i] = P[SUR_B3 + i];
     }
     for (int i = 0; i < SUR_OUT; ++i) bias[3 * SUR_H + i] = P[SUR_B4 + i];
+}
+
+void sur_make_tc_image(const float* P, uint16_t* img) {
+    std::memset(img, 0, TC_IMG_BYTES);
+    // element (n, k) of an N x K K-major matrix in 8 x 8 core matrices (no swizzle)
+    auto put = [&](int base, int K, int n, int k, float v) {
+        const int byte = base + (n >> 3) * (K / 8) * 128 + (k >> 3) * 128 + (n & 7) * 16 + (k & 7) * 2;
+        img[byte / 2] = bf16_bits(v);
+    };
+    // a bias as the two BF16 values whose sum the MMA forms in FP32
+    auto put_bias = [&](int base, int K, int n, int k, float b) {
+        const uint32_t u = uint32_t(bf16_bits(b)) << 16;
+        float hi;
+        std::memcpy(&hi, &u, 4);
+        put(base, K, n, k, b);
+        put(base, K, n, k + 1, b - hi);
+    };
+    for (int n = 0; n < SUR_H; ++n) {
+        for (int k = 0; k < 7; ++k) put(TC_B1, TC_K1, n, k, P[SUR_W1 + n * SUR_IN + k]);
+        put_bias(TC_B1, TC_K1, n, 7, P[SUR_B1 + n]);
+        for (int k = 0; k < SUR_H; ++k) {
+            put(TC_B2, TC_KH, n, k, P[SUR_W2 + n * SUR_H + k]);
+            put(TC_B3, TC_KH, n, k, P[SUR_W3 + n * SUR_H + k]);
+        }
+        put_bias(TC_B2, TC_KH, n, SUR_H, P[SUR_B2 + n]);
+        put_bias(TC_B3, TC_KH, n, SUR_H, P[SUR_B3 + n]);
+    }
+    for (int n = 0; n < SUR_OUT; ++n) {
+        for (int k = 0; k < SUR_H; ++k) put(TC_B4, TC_KH, n, k, P[SUR_W4 + n * SUR_H + k]);
+        put_bias(TC_B4, TC_KH, n, SUR_H, P[SUR_B4 + n]);
+    }
 }
 
 // ---------------------------------------------------------------- training data
@@ -145,9 +177,6 @@ constexpr int TRB = 32;          // samples per CTA
 constexpr int TRS = SUR_H + 1;   // transposed weight row stride (conflict-free both ways)
 
 __device__ __forceinline__ float bq(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
-__device__ __forceinline__ float gelu_acc(float z) {
-    return 0.5f * z * (1.0f + tanhf(GELU_K * (z + GELU_A * z * z * z)));
-}
 __device__ __forceinline__ float gelu_grad(float z) {
     const float t = tanhf(GELU_K * (z + GELU_A * z * z * z));
     return 0.5f * (1.0f + t) + 0.5f * z * (1.0f - t * t) * GELU_K * (1.0f + 3.0f * GELU_A * z * z);
@@ -166,7 +195,8 @@ struct TrainShared {
 };
 
 // Forward + backward of TRB samples per CTA (the quantised forward of the
-// tensor-core inference; the rounding is the identity in the backward pass).
+// tensor-core inference, its packed-BF16 GELU included; the rounding is the
+// identity in the backward pass, which differentiates the smooth GELU).
 // Each CTA writes its gradient sum and loss sum to part[blockIdx] (NPARAM + 1
 // floats): the reduction over CTAs happens in k_sur_adam in a fixed order.
 __global__ void __launch_bounds__(256) k_sur_fwd_bwd(const float* __restrict__ P, const float* __restrict__ X,
@@ -200,7 +230,10 @@ __global__ void __launch_bounds__(256) k_sur_fwd_bwd(const float* __restrict__ P
                 a1 = fmaf(wt[k * TRS + lane + 32], x, a1);
             }
             z[s * SUR_H + lane] = a0; z[s * SUR_H + lane + 32] = a1;
-            h[s * SUR_H + lane] = bq(gelu_acc(a0)); h[s * SUR_H + lane + 32] = bq(gelu_acc(a1));
+            // the inference's GELU (packed BF16 arithmetic), elementwise on the pair
+            const uint32_t g2 = gelu_pair<1>(a0, a1);
+            h[s * SUR_H + lane] = __uint_as_float(g2 << 16);
+            h[s * SUR_H + lane + 32] = __uint_as_float(g2 & 0xffff0000u);
         }
     };
     hidden(S.h0, SUR_IN, S.w1t, S.b, S.z1, S.h1);
@@ -337,6 +370,70 @@ __global__ void __launch_bounds__(128) k_sur_eval(const uint2* __restrict__ frag
         if (r0 < n) { Y[r0 * 8 + 2 * t] = out[0]; Y[r0 * 8 + 2 * t + 1] = out[1]; }
         if (r1 < n) { Y[r1 * 8 + 2 * t] = out[2]; Y[r1 * 8 + 2 * t + 1] = out[3]; }
     }
+}
+
+// The network on tcgen05: one 128-sample tile per CTA iteration (sur_tc.cuh).
+template <int GM>
+__global__ void __launch_bounds__(128) k_sur_eval_tc(const uint4* __restrict__ img_g, const float* __restrict__ X,
+                                                     size_t n, float* __restrict__ Y, int* __restrict__ err) {
+    extern __shared__ __align__(128) uint4 img_s[];
+    __shared__ uint32_t tmem_slot;
+    __shared__ __align__(8) uint64_t bar;
+    SurTc s;
+    sur_tc_setup(s, img_g, img_s, &tmem_slot, &bar);
+    const size_t ntiles = (n + 127) / 128;
+    for (size_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const size_t row = tile * 128 + threadIdx.x;
+        float4 x0 = make_float4(0, 0, 0, 0), x1 = x0;
+        if (row < n) {
+            x0 = reinterpret_cast<const float4*>(X)[row * 2];
+            x1 = reinterpret_cast<const float4*>(X)[row * 2 + 1];
+        }
+        const uint32_t in[8] = {pack_bf16x2(x0.x, x0.y), pack_bf16x2(x0.z, x0.w), pack_bf16x2(x1.x, x1.y),
+                                pack_bf16x2(x1.z, 1.0f), pack_bf16x2(1.0f, 0.0f), 0u, 0u, 0u};
+        float out[8];
+        if (!sur_tc_forward<GM>(s, in, out)) break;
+        if (row < n) {
+            reinterpret_cast<float4*>(Y)[row * 2] = make_float4(out[0], out[1], out[2], out[3]);
+            reinterpret_cast<float4*>(Y)[row * 2 + 1] = make_float4(out[4], out[5], out[6], out[7]);
+        }
+    }
+    if (!sur_tc_teardown(s) && threadIdx.x == 0) atomicExch(err, 1);
+}
+
+// the weight image on the device (TC_IMG_BYTES)
+int sur_upload_tc(const float* params_host_or_dev, void* img_dev, cudaStream_t st) {
+    std::vector<float> P(SUR_NPARAM);
+    if (is_device_ptr(params_host_or_dev)) {
+        TVGB_CUDA(cudaMemcpyAsync(P.data(), params_host_or_dev, SUR_NPARAM * 4, cudaMemcpyDeviceToHost, st));
+        TVGB_CUDA(cudaStreamSynchronize(st));
+    } else {
+        std::memcpy(P.data(), params_host_or_dev, SUR_NPARAM * 4);
+    }
+    std::vector<uint16_t> img(TC_IMG_BYTES / 2);
+    sur_make_tc_image(P.data(), img.data());
+    TVGB_CUDA(cudaMemcpyAsync(img_dev, img.data(), TC_IMG_BYTES, cudaMemcpyHostToDevice, st));
+    TVGB_CUDA(cudaStreamSynchronize(st));   // the host vector goes out of scope
+    return TVGB_OK;
+}
+
+int sur_eval_tc_device(const void* img, const float* X, size_t n, float* Y, int gelu_mode, int* err,
+                       cudaStream_t st) {
+    if (n == 0) return TVGB_OK;
+    const size_t tiles = (n + 127) / 128;
+    const unsigned grid = unsigned(tiles < 152 * 4 ? tiles : 152 * 4);
+    const int smem = TC_SMEM_PER_CTA;
+    const void* fn = gelu_mode == 0 ? (const void*)k_sur_eval_tc<0> : (const void*)k_sur_eval_tc<1>;
+    TVGB_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    const uint4* img4 = static_cast<const uint4*>(img);
+    void* args[] = {&img4, &X, &n, &Y, &err};
+    {
+        KernelTimer kt_("k_sur_eval_tc", st);
+        TVGB_CUDA(cudaLaunchKernel(fn, dim3(grid), dim3(128), args, smem, st));
+        kt_.stop();
+    }
+    TVGB_LAUNCHED();
+    return TVGB_OK;
 }
 
 int sur_upload(const float* params_host_or_dev, uint2* frag_dev, float* bias_dev, cudaStream_t st) {
@@ -499,6 +596,31 @@ int tvgb_surrogate_eval(const float* params, const float* X, size_t n, float* Y,
     TVGB_TRY(sur_eval_device(frag, bias, dx.get<float>(), n, dy.get<float>(), st));
     TVGB_TRY(dy.finish());
     return sync_if(dx.owned || dy.owned, st);
+}
+
+int tvgb_surrogate_eval_tc(const float* params, const float* X, size_t n, float* Y, int gelu_mode, void* stream) {
+    TVGB_CHECK_ARG(params && X && Y, "tvgb_surrogate_eval_tc: NULL pointer");
+    TVGB_CHECK_ARG(gelu_mode == 0 || gelu_mode == 1, "tvgb_surrogate_eval_tc: gelu_mode must be 0 or 1");
+    if (n == 0) return TVGB_OK;
+    cudaStream_t st = as_stream(stream);
+    DevArray dx, dy;
+    TVGB_TRY(dx.in(X, n * 32, st));
+    TVGB_TRY(dy.out(Y, n * 32, st, true));
+    Scratch net;
+    TVGB_TRY(net.alloc(TC_IMG_BYTES + 16, st));
+    int* err = reinterpret_cast<int*>(static_cast<char*>(net.p) + TC_IMG_BYTES);
+    TVGB_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
+    TVGB_TRY(sur_upload_tc(params, net.p, st));
+    TVGB_TRY(sur_eval_tc_device(net.p, dx.get<float>(), n, dy.get<float>(), gelu_mode, err, st));
+    int herr = 0;
+    TVGB_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    TVGB_TRY(dy.finish());
+    TVGB_CUDA(cudaStreamSynchronize(st));
+    if (herr) {
+        set_error("tvgb_surrogate_eval_tc: a tensor-core wait timed out");
+        return TVGB_ERR_CUDA;
+    }
+    return TVGB_OK;
 }
 
 }  // extern "C"

@@ -24,6 +24,9 @@ int simf2_device(const float4* A, const float4* B, size_t n, double* acc3, cudaS
 // (host or device), and its evaluation on n inputs (n x 8 floats)
 int sur_upload(const float* params, uint2* frag_dev, float* bias_dev, cudaStream_t s);
 int sur_eval_device(const uint2* frag, const float* bias, const float* X, size_t n, float* Y, cudaStream_t s);
+// the tcgen05 network (sur_tc.cuh): weight image upload and evaluation
+int sur_upload_tc(const float* params, void* img_dev, cudaStream_t s);
+int sur_eval_tc_device(const void* img, const float* X, size_t n, float* Y, int gelu_mode, int* err, cudaStream_t s);
 
 // window rule of the reference's Python layer (tensorvote_tk.cu:88-95)
 inline unsigned auto_window(float s1, float s2) {

@@ -1239,7 +1239,7 @@ extern "C" int tvgb_vote3_noalloc(const float* in, int in_layout, unsigned s0, u
 // The ball vote (lambda0 x the mean unit stick vote over the sphere) depends
 // on the offset only: it is tabulated per offset by the same rule (network
 // with flag 0 / closed form / 8 x 8 sphere rule) and applied per pair.
-#include "surrogate_mlp.cuh"
+#include "sur_tc.cuh"
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -1250,13 +1250,13 @@ enum { PLATE_SURROGATE = 0, PLATE_CLOSED = 1, PLATE_PLAIN64 = 2 };
 
 struct SurVoteArgs {
     FastArgs f;
-    const uint2* frag;        // network (PLATE_SURROGATE)
-    const float* bias;
+    const uint4* img;         // the network's weight image (PLATE_SURROGATE, sur_tc.cuh)
     const float* ball_tab;    // (2 hw + 1)^3 x 8 floats, or NULL
     const float* ball_exact;  // the exact ball table (the judge's), PLATE_SURROGATE only
     float inv_sig;
     float tol;
     unsigned* stats;          // [0] CTAs, [1] CTAs whose plate was recomputed exactly
+    int* err;                 // set when a tensor-core wait gave up
 };
 
 __constant__ float c_cs64[64], c_sn64[64];
@@ -1335,6 +1335,8 @@ __device__ __forceinline__ void plate_exact_sum(const SurVoteArgs& a, const floa
     }
 }
 
+// The exact plate rules (PLATE_CLOSED, PLATE_PLAIN64) in the surrogate
+// kernel's skeleton, for timing side by side with it.
 template <int MODE, bool STICK, bool BALL>
 __global__ void __launch_bounds__(128) k_vote3_sur(SurVoteArgs a) {
     extern __shared__ __align__(16) float4 sm4[];
@@ -1342,10 +1344,6 @@ __global__ void __launch_bounds__(128) k_vote3_sur(SurVoteArgs a) {
     const int hw = f.hw;
     const int nt = 3 * hw * hw + 1;
     float4* tbl = sm4;                                               // 2 nt float4
-    uint2* frag = reinterpret_cast<uint2*>(tbl + 2 * nt);            // SUR_NFRAG * 32
-    float* bias = reinterpret_cast<float*>(frag + SUR_NFRAG * 32);   // SUR_NBIAS
-    float* sacc = bias + SUR_NBIAS;                                  // 4 warps x 32 x 8
-    __shared__ int s_fail;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     for (int L2 = tid; L2 < nt; L2 += 128) {
         float4 ea, eb;
@@ -1353,21 +1351,13 @@ __global__ void __launch_bounds__(128) k_vote3_sur(SurVoteArgs a) {
         tbl[2 * L2] = ea;
         tbl[2 * L2 + 1] = eb;
     }
-    if (MODE == PLATE_SURROGATE) {
-        for (int e = tid; e < SUR_NFRAG * 32; e += 128) frag[e] = a.frag[e];
-        for (int e = tid; e < SUR_NBIAS; e += 128) bias[e] = a.bias[e];
-    }
-    if (tid == 0) s_fail = 0;
     __syncthreads();
 
     const int x = blockIdx.x * 32 + lane, y = blockIdx.y * 4 + warp, z = blockIdx.z;
     const bool yin = y < f.s1;
-    const int g = lane >> 2, t = lane & 3;
     const float4 Z4 = make_float4(0, 0, 0, 0);
     float tot[6], cmp[6];
     for (int k = 0; k < 6; ++k) { tot[k] = 0.0f; cmp[k] = 0.0f; }
-    float pl[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
-    float bs[6] = {0, 0, 0, 0, 0, 0};   // the network's ball (PLATE_SURROGATE), judged with the plate
     const int W = 2 * hw + 1;
     for (int oz = -hw; oz <= hw; ++oz) {
         const int vz = z + oz;
@@ -1392,41 +1382,13 @@ __global__ void __launch_bounds__(128) k_vote3_sur(SurVoteArgs a) {
                     const float4* bt = reinterpret_cast<const float4*>(
                         a.ball_tab + 8 * (size_t((oz + hw) * W + (oy + hw)) * W + (ox + hw)));
                     const float4 b0 = __ldg(bt), b1 = __ldg(bt + 1);
-                    float* D = MODE == PLATE_SURROGATE ? bs : P;
-                    D[0] = fmaf(lb, b0.x, D[0]); D[1] = fmaf(lb, b0.y, D[1]); D[2] = fmaf(lb, b0.z, D[2]);
-                    D[3] = fmaf(lb, b0.w, D[3]); D[4] = fmaf(lb, b1.x, D[4]); D[5] = fmaf(lb, b1.y, D[5]);
+                    P[0] = fmaf(lb, b0.x, P[0]); P[1] = fmaf(lb, b0.y, P[1]); P[2] = fmaf(lb, b0.z, P[2]);
+                    P[3] = fmaf(lb, b0.w, P[3]); P[4] = fmaf(lb, b1.x, P[4]); P[5] = fmaf(lb, b1.y, P[5]);
                 }
-                if (MODE == PLATE_CLOSED || L2 == 0) {
+                if (MODE == PLATE_CLOSED || L2 == 0)
                     vote_pair<false, true, false>(Z4, B, 0.0f, 0.0f, fmaf(B.x, oxf, B.y * oyf), oxf, oyf, ozf, ta, tb, P);
-                } else if (MODE == PLATE_PLAIN64) {
+                else
                     plate_plain64(B, oxf, oyf, ozf, ta, float(L2), P);
-                } else {
-                    // network input of row r (pair of lane r): (o / |o|, n_r, 1, 0); this lane holds
-                    // columns 2t, 2t + 1 of rows g, g + 8 of each 16-row tile
-                    const float il = rsqrtf(float(L2));
-                    const float ins[4] = {oxf * il, oyf * il, ozf * il, 0.0f};
-                    const float c1 = ta.x;
-#pragma unroll 1
-                    for (int T = 0; T < 2; ++T) {
-                        const int r0 = 16 * T + g, r1 = r0 + 8;
-                        const float n0x = __shfl_sync(0xffffffffu, B.x, r0), n0y = __shfl_sync(0xffffffffu, B.y, r0);
-                        const float n0z = __shfl_sync(0xffffffffu, B.z, r0), s0w = __shfl_sync(0xffffffffu, B.w, r0);
-                        const float n1x = __shfl_sync(0xffffffffu, B.x, r1), n1y = __shfl_sync(0xffffffffu, B.y, r1);
-                        const float n1z = __shfl_sync(0xffffffffu, B.z, r1), s1w = __shfl_sync(0xffffffffu, B.w, r1);
-                        float lo0, hi0, lo1, hi1;
-                        if (t == 0) { lo0 = ins[0]; hi0 = ins[1]; lo1 = ins[0]; hi1 = ins[1]; }
-                        else if (t == 1) { lo0 = ins[2]; hi0 = n0x; lo1 = ins[2]; hi1 = n1x; }
-                        else if (t == 2) { lo0 = n0y; hi0 = n0z; lo1 = n1y; hi1 = n1z; }
-                        else { lo0 = 1.0f; hi0 = 0.0f; lo1 = 1.0f; hi1 = 0.0f; }
-                        const uint32_t fin[4] = {pack_bf16x2(lo0, hi0), pack_bf16x2(lo1, hi1), 0u, 0u};
-                        float out[4];
-                        sur_mlp16(frag, bias, fin, out);
-                        const float w0 = s0w * c1, w1 = s1w * c1;
-                        float* acc = T == 0 ? pl[0] : pl[1];
-                        acc[0] = fmaf(w0, out[0], acc[0]); acc[1] = fmaf(w0, out[1], acc[1]);
-                        acc[2] = fmaf(w1, out[2], acc[2]); acc[3] = fmaf(w1, out[3], acc[3]);
-                    }
-                }
             }
         }
         kahan_add(tot[0], cmp[0], P[0] + P[6]);
@@ -1436,47 +1398,151 @@ __global__ void __launch_bounds__(128) k_vote3_sur(SurVoteArgs a) {
         kahan_add(tot[4], cmp[4], P[4]);
         kahan_add(tot[5], cmp[5], P[5] + P[6]);
     }
-    float plate[6] = {0, 0, 0, 0, 0, 0};
-    if (MODE == PLATE_SURROGATE) {
-        float* my = sacc + warp * 32 * 8;
-#pragma unroll
-        for (int T = 0; T < 2; ++T) {
-            my[(16 * T + g) * 8 + 2 * t] = pl[T][0];
-            my[(16 * T + g) * 8 + 2 * t + 1] = pl[T][1];
-            my[(16 * T + g + 8) * 8 + 2 * t] = pl[T][2];
-            my[(16 * T + g + 8) * 8 + 2 * t + 1] = pl[T][3];
-        }
-        __syncwarp();
-        for (int k = 0; k < 6; ++k) plate[k] = my[lane * 8 + k] + bs[k];
-        // judge: the first warp's receivers against the exact plate (and ball)
-        const bool mine = x < f.s2 && yin;
-        if (warp == 0) {
-            float E[7];
-            plate_exact_sum<BALL>(a, tbl, x, y, z, E);
-            const float e6[6] = {E[0] + E[6], E[1], E[2], E[3] + E[6], E[4], E[5] + E[6]};
-            float dn = 0.0f, tn = 0.0f;
-            for (int k = 0; k < 6; ++k) {
-                const float wgt = (k == 0 || k == 3 || k == 5) ? 1.0f : 2.0f;
-                const float d = plate[k] - e6[k], tt = tot[k] + e6[k];
-                dn = fmaf(wgt * d, d, dn);
-                tn = fmaf(wgt * tt, tt, tn);
-            }
-            const bool bad = mine && !(dn <= a.tol * a.tol * tn);
-            if (__any_sync(0xffffffffu, bad) && lane == 0) s_fail = 1;
-        }
-        __syncthreads();
-        if (s_fail) {
-            float E[7];
-            plate_exact_sum<BALL>(a, tbl, x, y, z, E);
-            plate[0] = E[0] + E[6]; plate[1] = E[1]; plate[2] = E[2];
-            plate[3] = E[3] + E[6]; plate[4] = E[4]; plate[5] = E[5] + E[6];
-        }
-        if (tid == 0 && a.stats) {
-            atomicAdd(a.stats, 1u);
-            if (s_fail) atomicAdd(a.stats + 1, 1u);
-        }
-    }
     if (x >= f.s2 || !yin) return;
+    const size_t plane = size_t(f.s1) * f.s2, n = size_t(f.s0) * plane;
+    write_receiver(f, size_t(z) * plane + size_t(y) * f.s2 + x, n, tot);
+}
+
+// The surrogate vote on the tensor cores.  A CTA is 32 x 4 receivers (one per
+// thread, = one row of the M = 128 tile); for each voter offset o != 0 the
+// CTA runs one tile through the network (sur_tc.cuh): row r holds (o / |o|,
+// n of receiver r's voter, 1).  Offsets are visited in the same order by
+// every thread (the tile's MMAs synchronise the CTA): rows whose voter lies
+// outside the volume carry a zero record and vote zero.  While the tensor
+// core runs layer 1, the same threads vote the stick exactly.  The network's
+// plate (and ball) accumulate apart from the exact terms, so that the judge
+// can compare them with the exact plate of the CTA's first 32 receivers.
+template <bool STICK, bool BALL>
+__global__ void __launch_bounds__(128) k_vote3_surtc(SurVoteArgs a) {
+    extern __shared__ __align__(128) float4 sm4[];
+    const FastArgs& f = a.f;
+    const int hw = f.hw;
+    const int nt = 3 * hw * hw + 1;
+    uint4* img_s = reinterpret_cast<uint4*>(sm4);                    // weight image
+    float4* tbl = sm4 + TC_IMG_BYTES / 16;                           // 2 nt float4
+    __shared__ uint32_t tmem_slot;
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ int s_fail;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int L2 = tid; L2 < nt; L2 += 128) {
+        float4 ea, eb;
+        radial_entry(L2, f.sig1, f.sig2, ea, eb);
+        tbl[2 * L2] = ea;
+        tbl[2 * L2 + 1] = eb;
+    }
+    if (tid == 0) s_fail = 0;
+    SurTc tcs;
+    sur_tc_setup(tcs, a.img, img_s, &tmem_slot, &bar);   // ends with __syncthreads
+
+    const int x = blockIdx.x * 32 + lane, y = blockIdx.y * 4 + warp, z = blockIdx.z;
+    const int y0 = blockIdx.y * 4;
+    const bool yin = y < f.s1;
+    const float4 Z4 = make_float4(0, 0, 0, 0);
+    const uint32_t tA = tcs.tmem + tc_lane_base() + TC_A, tD = tcs.tmem + tc_lane_base() + TC_D;
+    float tot[6], cmp[6], net[6], bs[6];
+    for (int k = 0; k < 6; ++k) { tot[k] = 0.0f; cmp[k] = 0.0f; net[k] = 0.0f; bs[k] = 0.0f; }
+    const int W = 2 * hw + 1;
+    // rows oy for which any of the CTA's 4 receiver rows has its voter inside the volume
+    const int oy_lo = max(-hw, -(y0 + 3)), oy_hi = min(hw, f.s1 - 1 - y0);
+    bool ok = true;
+    for (int oz = -hw; oz <= hw && ok; ++oz) {
+        const int vz = z + oz;
+        if ((unsigned)vz >= (unsigned)f.s0) continue;                // CTA-uniform
+        float P[7] = {0, 0, 0, 0, 0, 0, 0};
+        float Q[6] = {0, 0, 0, 0, 0, 0};
+        for (int oy = oy_lo; oy <= oy_hi && ok; ++oy) {
+            const int vy = y + oy;
+            const bool rin = yin && (unsigned)vy < (unsigned)f.s1;
+            const size_t row = (size_t(vz) * f.s1 + (rin ? vy : 0)) * f.s2;
+            for (int ox = -hw; ox <= hw; ++ox) {
+                const int vx = x + ox;
+                const bool in = rin && (unsigned)vx < (unsigned)f.s2;
+                const float4 A = (STICK && in) ? __ldg(f.A + row + vx) : Z4;
+                const float4 B = in ? __ldg(f.B + row + vx) : Z4;
+                const int L2 = ox * ox + oy * oy + oz * oz;
+                const float4 ta = tbl[2 * L2], tb = tbl[2 * L2 + 1];
+                const float oxf = float(ox), oyf = float(oy), ozf = float(oz);
+                if (L2 == 0) {                                       // CTA-uniform: o = 0 is voted exactly
+                    if (STICK)
+                        vote_pair<true, false, false>(A, Z4, 0.0f, fmaf(A.x, oxf, A.y * oyf), 0.0f, oxf, oyf, ozf, ta,
+                                                      tb, P);
+                    vote_pair<false, true, false>(Z4, B, 0.0f, 0.0f, fmaf(B.x, oxf, B.y * oyf), oxf, oyf, ozf, ta, tb, P);
+                } else {
+                    const float il = rsqrtf(float(L2));
+                    const uint32_t in8[8] = {pack_bf16x2(oxf * il, oyf * il), pack_bf16x2(ozf * il, B.x),
+                                             pack_bf16x2(B.y, B.z), pack_bf16x2(1.0f, 1.0f),
+                                             pack_bf16x2(1.0f, 0.0f), 0u, 0u, 0u};
+                    tc::tmem_st8(tA, in8);
+                    if (!sur_tc_layer<1>(tcs)) { ok = false; break; }
+                    // the exact stick vote while layer 1 runs
+                    if (STICK)
+                        vote_pair<true, false, false>(A, Z4, 0.0f, fmaf(A.x, oxf, A.y * oyf), 0.0f, oxf, oyf, ozf, ta,
+                                                      tb, P);
+                    sur_tc_hidden<1>(tcs);
+                    if (!sur_tc_layer<2>(tcs)) { ok = false; break; }
+                    sur_tc_hidden<1>(tcs);
+                    if (!sur_tc_layer<3>(tcs)) { ok = false; break; }
+                    sur_tc_hidden<1>(tcs);
+                    if (!sur_tc_layer<4>(tcs)) { ok = false; break; }
+                    uint32_t r[16];
+                    tc::tmem_ld16(tD, r);
+                    const float w = B.w * ta.x;                      // plate scale x c1(|o|)
+#pragma unroll
+                    for (int k = 0; k < 6; ++k) Q[k] = fmaf(w, __uint_as_float(r[k]), Q[k]);
+                }
+                if (BALL) {   // the tabulated ball (network, exact at o = 0), judged with the plate
+                    const float lb = in ? __ldg(f.C + row + vx) : 0.0f;
+                    const float4* bt = reinterpret_cast<const float4*>(
+                        a.ball_tab + 8 * (size_t((oz + hw) * W + (oy + hw)) * W + (ox + hw)));
+                    const float4 b0 = __ldg(bt), b1 = __ldg(bt + 1);
+                    bs[0] = fmaf(lb, b0.x, bs[0]); bs[1] = fmaf(lb, b0.y, bs[1]); bs[2] = fmaf(lb, b0.z, bs[2]);
+                    bs[3] = fmaf(lb, b0.w, bs[3]); bs[4] = fmaf(lb, b1.x, bs[4]); bs[5] = fmaf(lb, b1.y, bs[5]);
+                }
+            }
+        }
+        // exact terms (stick, o = 0 plate) into the Kahan sums; the network's plate apart
+        kahan_add(tot[0], cmp[0], P[0] + P[6]);
+        kahan_add(tot[1], cmp[1], P[1]);
+        kahan_add(tot[2], cmp[2], P[2]);
+        kahan_add(tot[3], cmp[3], P[3] + P[6]);
+        kahan_add(tot[4], cmp[4], P[4]);
+        kahan_add(tot[5], cmp[5], P[5] + P[6]);
+        for (int k = 0; k < 6; ++k) net[k] += Q[k];
+    }
+    if (!sur_tc_teardown(tcs) || !ok) {
+        if (tid == 0) atomicExch(a.err, 1);
+        return;
+    }
+    float plate[6];
+    for (int k = 0; k < 6; ++k) plate[k] = net[k] + bs[k];
+    // judge: the first warp's receivers against the exact plate (and ball)
+    const bool mine = x < f.s2 && yin;
+    if (warp == 0) {
+        float E[7];
+        plate_exact_sum<BALL>(a, tbl, x, y, z, E);
+        const float e6[6] = {E[0] + E[6], E[1], E[2], E[3] + E[6], E[4], E[5] + E[6]};
+        float dn = 0.0f, tn = 0.0f;
+        for (int k = 0; k < 6; ++k) {
+            const float wgt = (k == 0 || k == 3 || k == 5) ? 1.0f : 2.0f;
+            const float d = plate[k] - e6[k], tt = tot[k] + e6[k];
+            dn = fmaf(wgt * d, d, dn);
+            tn = fmaf(wgt * tt, tt, tn);
+        }
+        const bool bad = mine && !(dn <= a.tol * a.tol * tn);
+        if (__any_sync(0xffffffffu, bad) && lane == 0) s_fail = 1;
+    }
+    __syncthreads();
+    if (s_fail) {
+        float E[7];
+        plate_exact_sum<BALL>(a, tbl, x, y, z, E);
+        plate[0] = E[0] + E[6]; plate[1] = E[1]; plate[2] = E[2];
+        plate[3] = E[3] + E[6]; plate[4] = E[4]; plate[5] = E[5] + E[6];
+    }
+    if (tid == 0 && a.stats) {
+        atomicAdd(a.stats, 1u);
+        if (s_fail) atomicAdd(a.stats + 1, 1u);
+    }
+    if (!mine) return;
     const size_t plane = size_t(f.s1) * f.s2, n = size_t(f.s0) * plane;
     float m6[6];
     for (int k = 0; k < 6; ++k) m6[k] = tot[k] + plate[k];
@@ -1528,16 +1594,23 @@ __global__ void k_ball_table(int hw, float sig1, float sig2, float inv_sig, cons
 template <int MODE>
 static int launch_sur(const SurVoteArgs& a, bool S, bool B, dim3 grid, size_t smem, cudaStream_t st) {
     const void* fn;
-    if (S && B) fn = (const void*)k_vote3_sur<MODE, true, true>;
-    else if (S) fn = (const void*)k_vote3_sur<MODE, true, false>;
-    else if (B) fn = (const void*)k_vote3_sur<MODE, false, true>;
-    else fn = (const void*)k_vote3_sur<MODE, false, false>;
+    if (MODE == PLATE_SURROGATE) {
+        if (S && B) fn = (const void*)k_vote3_surtc<true, true>;
+        else if (S) fn = (const void*)k_vote3_surtc<true, false>;
+        else if (B) fn = (const void*)k_vote3_surtc<false, true>;
+        else fn = (const void*)k_vote3_surtc<false, false>;
+    } else {
+        if (S && B) fn = (const void*)k_vote3_sur<MODE, true, true>;
+        else if (S) fn = (const void*)k_vote3_sur<MODE, true, false>;
+        else if (B) fn = (const void*)k_vote3_sur<MODE, false, true>;
+        else fn = (const void*)k_vote3_sur<MODE, false, false>;
+    }
     TVGB_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     SurVoteArgs arg = a;
     void* args[] = {&arg};
     {
-        KernelTimer kt_(MODE == PLATE_SURROGATE ? "k_vote3_sur" : (MODE == PLATE_CLOSED ? "k_vote3_sur_closed"
-                                                                                       : "k_vote3_sur_plain64"), st);
+        KernelTimer kt_(MODE == PLATE_SURROGATE ? "k_vote3_surtc" : (MODE == PLATE_CLOSED ? "k_vote3_sur_closed"
+                                                                                         : "k_vote3_sur_plain64"), st);
         TVGB_CUDA(cudaLaunchKernel(fn, grid, dim3(128), args, smem, st));
         kt_.stop();
     }
@@ -1617,11 +1690,13 @@ extern "C" int tvgb_vote3_surrogate(const float* in, int in_layout, unsigned s0,
     fa.precise_eig = p->parity ? 0 : 1;
     a.inv_sig = 1.0f / p->sigma1;
     a.tol = tol;
+    // the network's weight image, then an error flag for the tensor-core waits
+    TVGB_TRY(snet.alloc(TC_IMG_BYTES + 16, st));
+    a.err = reinterpret_cast<int*>(static_cast<char*>(snet.p) + TC_IMG_BYTES);
+    TVGB_CUDA(cudaMemsetAsync(a.err, 0, sizeof(int), st));
     if (plate_mode == PLATE_SURROGATE) {
-        TVGB_TRY(snet.alloc(SUR_NFRAG * 32 * sizeof(uint2) + SUR_NBIAS * 4, st));
-        a.frag = snet.get<uint2>();
-        a.bias = reinterpret_cast<float*>(snet.get<uint2>() + SUR_NFRAG * 32);
-        TVGB_TRY(sur_upload(net_params, const_cast<uint2*>(a.frag), const_cast<float*>(a.bias), st));
+        a.img = snet.get<uint4>();
+        TVGB_TRY(sur_upload_tc(net_params, snet.p, st));
     }
     if (B) {
         const size_t nt3 = size_t(W) * W * W;
@@ -1639,7 +1714,7 @@ extern "C" int tvgb_vote3_surrogate(const float* in, int in_layout, unsigned s0,
             TVGB_TRY(sX.alloc(nt3 * 32, st));
             TVGB_TRY(sY.alloc(nt3 * 32, st));
             TVGB_CUDA(cudaMemcpyAsync(sX.p, X.data(), nt3 * 32, cudaMemcpyHostToDevice, st));
-            TVGB_TRY(sur_eval_device(a.frag, a.bias, sX.get<float>(), nt3, sY.get<float>(), st));
+            TVGB_TRY(sur_eval_tc_device(snet.p, sX.get<float>(), nt3, sY.get<float>(), 1, a.err, st));
             TVGB_CUDA(cudaStreamSynchronize(st));   // X leaves scope
             Fnet = sY.get<float>();
         }
@@ -1664,18 +1739,30 @@ extern "C" int tvgb_vote3_surrogate(const float* in, int in_layout, unsigned s0,
     TVGB_CUDA(cudaMemsetAsync(sst.p, 0, 16, st));
     a.stats = sst.get<unsigned>();
     const int nt = 3 * hw * hw + 1;
-    const size_t smem = size_t(2) * nt * 16 + SUR_NFRAG * 32 * sizeof(uint2) + SUR_NBIAS * 4 + 4 * 32 * 8 * 4;
+    size_t smem = size_t(2) * nt * 16;
+    if (plate_mode == PLATE_SURROGATE) {
+        // the weight image before the radial table; at least TC_SMEM_PER_CTA, so
+        // that no more CTAs share an SM than its tensor memory holds
+        smem += TC_IMG_BYTES;
+        if (smem < size_t(TC_SMEM_PER_CTA)) smem = TC_SMEM_PER_CTA;
+    }
     TVGB_CHECK_ARG(smem <= 200 * 1024, "tvgb_vote3_surrogate: window w = %u too large", w);
     dim3 grid(ceil_div(s2, 32u), ceil_div(s1, 4u), s0);
     if (plate_mode == PLATE_SURROGATE) TVGB_TRY(launch_sur<PLATE_SURROGATE>(a, S, B, grid, smem, st));
     else if (plate_mode == PLATE_CLOSED) TVGB_TRY(launch_sur<PLATE_CLOSED>(a, S, B, grid, smem, st));
     else TVGB_TRY(launch_sur<PLATE_PLAIN64>(a, S, B, grid, smem, st));
     unsigned hst[2] = {0, 0};
+    int herr = 0;
     TVGB_CUDA(cudaMemcpyAsync(hst, sst.p, 8, cudaMemcpyDeviceToHost, st));
+    TVGB_CUDA(cudaMemcpyAsync(&herr, a.err, sizeof(int), cudaMemcpyDeviceToHost, st));
     TVGB_TRY(dout.finish());
     TVGB_TRY(dev_.finish());
     TVGB_TRY(dvec.finish());
     TVGB_CUDA(cudaStreamSynchronize(st));
+    if (herr) {
+        set_error("tvgb_vote3_surrogate: a tensor-core wait timed out");
+        return TVGB_ERR_CUDA;
+    }
     if (stats) { stats[0] = hst[0]; stats[1] = hst[1]; }
     return TVGB_OK;
 }

@@ -108,12 +108,26 @@ def train(params, X, T, batch=8192, steps=2000, lr=2e-3, history=True):
     return hist
 
 
-def evaluate(params, X):
-    """The network's outputs (n x 8, 6 used) on the tensor cores."""
+_GELU = {"fp32": 0, "bf16": 1}
+
+
+def evaluate(params, X, engine="tcgen05", gelu="bf16"):
+    """The network's outputs (n x 8, 6 used) on the tensor cores.  engine
+    "tcgen05" (tensor memory; gelu "bf16", the packed arithmetic the network
+    is trained with and the vote uses, or "fp32") or "mma" (warp-level
+    mma.sync, GELU in FP32; a cross-check of the tcgen05 path)."""
     X = _api._check_f32(X, "X")
     Y = _api._empty_like_kind(X, (int(X.shape[0]), 8))
-    _api.call("tvgb_surrogate_eval", _api._ptr(_api._check_f32(params, "params")), _api._ptr(X), int(X.shape[0]),
-              _api._ptr(Y), _api._stream_for(X, Y))
+    P = _api._ptr(_api._check_f32(params, "params"))
+    if engine == "tcgen05":
+        _api.call("tvgb_surrogate_eval_tc", P, _api._ptr(X), int(X.shape[0]), _api._ptr(Y), _GELU[gelu],
+                  _api._stream_for(X, Y))
+    elif engine == "mma":
+        if gelu != "fp32":
+            raise ValueError("the mma engine computes the GELU in FP32 only")
+        _api.call("tvgb_surrogate_eval", P, _api._ptr(X), int(X.shape[0]), _api._ptr(Y), _api._stream_for(X, Y))
+    else:
+        raise ValueError(f"engine must be 'tcgen05' or 'mma', not {engine!r}")
     return Y
 
 
