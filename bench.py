@@ -20,6 +20,10 @@ whole pass over the volume; the metric is voxels per second.
   cpu_baseline  the reference's CPU algorithm (the C port in oracle/, the
             reference's own sampled plate rule) on a bounded interior sample,
             all host cores, rank 0 at N = 1 only.
+  surrogate the learned plate vote against the plain 64-orientation integral
+            and the exact closed form on an interior block of the same field
+            (network trained first, on the GPU): voxels/s of each, their
+            ratios, errors against the exact vote, the judge's recomputes.
 
 --impl reference runs that CPU reference alone (rank 0), one bounded sample
 per step.  Under torchrun every rank processes its own volume (weak scaling,
@@ -410,6 +414,10 @@ def run_ours(args, rank, world, local_rank):
                     "flops_per_launch": flops, "avg_launch_ms": avg_s * 1e3,
                     "share_of_step": (tot_ms / (np.sum(times))) if np.sum(times) else None}
 
+    sur = None
+    if rank == 0 and world == 1 and not args.no_surrogate and not strong:
+        sur = surrogate_study(vol_d, cfg, args, dev)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         t, nrec, th = cpu_reference_sample(vol_np, cfg, block=args.ref_block, seed=0)
@@ -428,12 +436,83 @@ def run_ours(args, rank, world, local_rank):
             "e2e": {"value": e2e_value, "unit": "voxels/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
             "kernels": {k: {"launches": v[0], "total_ms": v[1]} for k, v in prof.items()},
-            "memory": memory,
+            "memory": memory, "surrogate": sur,
         }
         print(json.dumps(line), flush=True)
     if dist:
         dist.barrier()
         dist.destroy_process_group()
+
+
+# ----------------------------------------------------------------------------- surrogate vs plain
+
+def surrogate_study(vol_d, cfg, args, dev):
+    """The learned plate vote against the plain 64-orientation integral and
+    the exact closed form, in the same kernel skeleton, on a bounded interior
+    block of the benchmark's own field (the structure tensor of the whole
+    volume, cropped): stick exact in every mode, plate by the rule named.
+    The network (7 -> 64 -> 64 -> 64 -> 6, BF16 on tcgen05) is trained first,
+    on the GPU, on 2^24 samples of the plain integral.  Errors are against
+    the closed form, the exact integral (within 2e-6 of the FP64 oracle)."""
+    import ctypes
+    import torch
+    import tiralib_gb300 as tv
+    from tiralib_gb300 import surrogate as S
+    lib = tv.lib()
+    b = min(args.sur_block, cfg["n"])
+    lo = (cfg["n"] - b) // 2
+    F = tv.structure_tensor3(vol_d, cfg["sigma_st"], mode="same", layout="mat3")
+    F = F[lo:lo + b, lo:lo + b, lo:lo + b].contiguous()
+    t0 = time.perf_counter()
+    X, T = S.samples(1 << 24, seed=4, device=dev)
+    p = S.init_params(0)
+    hist = S.train(p, X, T, batch=8192, steps=args.sur_steps, lr=3e-3)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    del X, T
+    Xh, Th = S.samples(1 << 16, seed=77)
+    Yh = S.evaluate(p, Xh)
+    heldout = float(np.linalg.norm(Yh[:, :6] - Th[:, :6]) / np.linalg.norm(Th[:, :6]))
+    buf = ctypes.create_string_buffer(1 << 14)
+    kname = {"closed": "k_vote3_sur_closed", "plain64": "k_vote3_sur_plain64", "surrogate": "k_vote3_surtc"}
+    runs = {"closed": ("closed", 1e-3), "plain64": ("plain64", 1e-3), "surrogate_judged": ("surrogate", 1e-3),
+            "surrogate_unjudged": ("surrogate", float("inf"))}
+    res, kms, stats = {}, {}, {}
+    for key, (mode, tol) in runs.items():
+        S.vote3(F, cfg["sigma"], params=p, mode=mode, tol=tol, w=cfg["w"])      # warm-up
+        lib.tvgb_profile_enable(1)
+        lib.tvgb_profile_read(buf, len(buf))
+        reps = 2
+        for _ in range(reps):
+            o, _, _, st = S.vote3(F, cfg["sigma"], params=p, mode=mode, tol=tol, w=cfg["w"])
+        torch.cuda.synchronize()
+        lib.tvgb_profile_read(buf, len(buf))
+        lib.tvgb_profile_enable(0)
+        nl, ms = parse_profile(buf.value.decode()).get(kname[mode], (0, 0.0))
+        kms[key] = ms / max(nl, 1)
+        res[key] = o.cpu().numpy().reshape(-1, 9)[:, [0, 1, 2, 4, 5, 8]].astype(np.float64)
+        stats[key] = st
+    ex = res["closed"]
+    nex = np.linalg.norm(ex)
+    err = {k: {"normwise": float(np.linalg.norm(v - ex) / nex), "max_abs_over_max": float(np.abs(v - ex).max() /
+                                                                                         np.abs(ex).max())}
+           for k, v in res.items() if k != "closed"}
+    vps = {k: b ** 3 / (v / 1e3) for k, v in kms.items()}
+    return {
+        "sample": f"{b}^3 interior block of this field (structure tensor of the whole volume, cropped), sigma "
+                  f"{cfg['sigma']:g}, w {cfg['w']}; stick exact, plate by the rule named; ball off",
+        "network": f"7-64-64-64-6 GELU, BF16 weights and activations, FP32 accumulation, tcgen05.mma with the "
+                   f"activations in tensor memory; trained here on 2^24 plain-integral samples, {args.sur_steps} "
+                   f"Adam steps of 8192",
+        "train_s": t_train, "final_loss": float(np.mean(hist[-100:])), "heldout_rel_err": heldout,
+        "kernel_ms": kms, "voxels_per_s": vps,
+        "surrogate_vs_plain64": vps["surrogate_unjudged"] / vps["plain64"],
+        "surrogate_judged_vs_plain64": vps["surrogate_judged"] / vps["plain64"],
+        "closed_vs_plain64": vps["closed"] / vps["plain64"],
+        "rel_err_vs_exact": err,
+        "judge": {"tol": 1e-3, "ctas": int(stats["surrogate_judged"][0]),
+                  "recomputed_exactly": int(stats["surrogate_judged"][1])},
+    }
 
 
 # ----------------------------------------------------------------------------- C3: batched 3x3 eigen
@@ -805,6 +884,9 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--ref-block", type=int, default=12, help="edge of the CPU reference's receiver block")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-surrogate", action="store_true", help="skip the surrogate-vs-plain study")
+    ap.add_argument("--sur-block", type=int, default=64, help="edge of the surrogate study's interior block")
+    ap.add_argument("--sur-steps", type=int, default=40000, help="Adam steps of the surrogate's training")
     ap.add_argument("--config", choices=["c2", "c4", "c5", "c3", "c1"], default="c2",
                     help="c2: 3D pipeline, 256^3 (the headline); c4: the same at 384^3; c5: 512^3 tubes + sheets, "
                          "sigma 6, stick + plate + ball (capacity); c3: batched 3x3 eigen; c1: 2D pipeline")
