@@ -138,3 +138,55 @@ def test_surrogate_vote_and_its_judge(S, trained):
     # without the network the mode is refused
     with pytest.raises(tv.TvgbError):
         S.vote3(F, 2.0, params=None, mode="surrogate")
+
+
+def _kernel_ms(fn, name):
+    """Library-timed duration (ms) of the named kernel over one call of fn."""
+    import ctypes
+    import tiralib_gb300 as tv
+    lib = tv.lib()
+    buf = ctypes.create_string_buffer(1 << 14)
+    lib.tvgb_profile_enable(1)
+    lib.tvgb_profile_read(buf, len(buf))
+    out = fn()
+    lib.tvgb_profile_read(buf, len(buf))
+    lib.tvgb_profile_enable(0)
+    for line in buf.value.decode().splitlines():
+        parts = line.split()
+        if len(parts) == 3 and parts[0] == name:
+            return float(parts[2]) / int(parts[1]), out
+    raise AssertionError(f"{name} was not launched")
+
+
+def test_what_the_trained_network_gains(S):
+    """The learned plate vote against the method it stands in for, the plain
+    64-orientation integral, in the same kernel skeleton: speed of each, and
+    the network's vote error against the exact vote, trained and untrained.
+    On GB300 the network's 192 GELUs per pair (tanh on the MUFU pipe, 16 per
+    SM clock) cost about what the plain integral's ~1600 FP32 operations per
+    pair cost on the FMA pipe, so the measured speed ratio is near 1; the
+    test records it and bounds it from below."""
+    import torch
+    dev = torch.device("cuda:0")
+    X, T = S.samples(1 << 22, seed=4, device=dev)
+    trained = S.init_params(0)
+    S.train(trained, X, T, batch=8192, steps=20000, lr=3e-3)
+    untrained = S.init_params(0)
+    F = _field(3, shape=(32, 40, 48))
+    exact, _, _, _ = S.vote3(F, 4.0, mode="closed")
+    S.vote3(F, 4.0, mode="plain64")                                   # warm-up
+    S.vote3(F, 4.0, params=trained, mode="surrogate", tol=float("inf"))
+    t_plain, (plain, _, _, _) = _kernel_ms(lambda: S.vote3(F, 4.0, mode="plain64"), "k_vote3_sur_plain64")
+    t_net, (net, _, _, st) = _kernel_ms(lambda: S.vote3(F, 4.0, params=trained, mode="surrogate",
+                                                       tol=float("inf")), "k_vote3_surtc")
+    raw, _, _, _ = S.vote3(F, 4.0, params=untrained, mode="surrogate", tol=float("inf"))
+    nrm = np.linalg.norm(exact)
+    e_plain = np.linalg.norm(plain - exact) / nrm
+    e_net = np.linalg.norm(net - exact) / nrm
+    e_raw = np.linalg.norm(raw - exact) / nrm
+    print(f"plain64 {t_plain:.2f} ms (err {e_plain:.1e}), network {t_net:.2f} ms (err {e_net:.1e}, untrained "
+          f"{e_raw:.1e}): speed ratio {t_plain / t_net:.2f}")
+    assert st[1] == 0                       # no judge: every plate by the network
+    assert e_plain < 1e-5
+    assert e_net < 2e-2 and e_net < 0.1 * e_raw
+    assert t_plain / t_net > 0.5

@@ -559,6 +559,59 @@ __device__ __forceinline__ void vote_row_pk(const float4* __restrict__ rA, const
     }
 }
 
+// both receiver pairs of a thread on one voter row: each voter record and its
+// (q.o, n.o) partial sums are read / formed once for the two pairs
+#ifndef TVGB_PK_FUSE
+#define TVGB_PK_FUSE 1         // both receiver pairs per voter-row pass
+#endif
+template <bool STICK, bool PLATE, bool BALL>
+__device__ __forceinline__ void vote_row_pk2(const float4* __restrict__ rA, const float4* __restrict__ rB,
+                                             const float* __restrict__ rC, const float4* __restrict__ pt0,
+                                             const float4* __restrict__ pt1, int NQ, const float2& oz20,
+                                             const float2& oz21, float oyf, int L2y, int hw, float2 (&P0)[7],
+                                             float2 (&P1)[7]) {
+    const float4 Z4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const float2 oy2 = bc2(oyf);
+    {   // ox = 0
+        const float4 A = STICK ? rA[0] : Z4, B = PLATE ? rB[0] : Z4;
+        const float lb = BALL ? rC[0] : 0.0f;
+        const float ub = A.y * oyf, vb = B.y * oyf;
+        const float4* e0 = pt0 + NQ * L2y;
+        const float4* e1 = pt1 + NQ * L2y;
+        vote_pair_pk<STICK, PLATE, BALL>(A, B, lb, ub, vb, bc2(0.0f), oy2, oz20, e0[0], e0[1], e0[2],
+                                         BALL ? e0[3] : Z4, P0);
+        vote_pair_pk<STICK, PLATE, BALL>(A, B, lb, ub, vb, bc2(0.0f), oy2, oz21, e1[0], e1[1], e1[2],
+                                         BALL ? e1[3] : Z4, P1);
+    }
+    float oxf = 1.0f;
+    int e2 = 1 + L2y;
+    int step = 3;                        // (ox + 1)^2 - ox^2 for ox = 1
+#pragma unroll 1
+    for (int d = 1; d <= hw; ++d) {
+        const float4 Ap = STICK ? rA[d] : Z4, Am = STICK ? rA[-d] : Z4;
+        const float4 Bp = PLATE ? rB[d] : Z4, Bm = PLATE ? rB[-d] : Z4;
+        const float lp = BALL ? rC[d] : 0.0f, lm = BALL ? rC[-d] : 0.0f;
+        const float ubp = fmaf(Ap.x, oxf, Ap.y * oyf), ubm = fmaf(-Am.x, oxf, Am.y * oyf);
+        const float vbp = fmaf(Bp.x, oxf, Bp.y * oyf), vbm = fmaf(-Bm.x, oxf, Bm.y * oyf);
+        const float2 oxp = bc2(oxf), oxm = bc2(-oxf);
+        {
+            const float4* e = pt0 + NQ * e2;
+            const float4 X = e[0], Y = e[1], Zt = e[2], W = BALL ? e[3] : Z4;
+            vote_pair_pk<STICK, PLATE, BALL>(Ap, Bp, lp, ubp, vbp, oxp, oy2, oz20, X, Y, Zt, W, P0);
+            vote_pair_pk<STICK, PLATE, BALL>(Am, Bm, lm, ubm, vbm, oxm, oy2, oz20, X, Y, Zt, W, P0);
+        }
+        {
+            const float4* e = pt1 + NQ * e2;
+            const float4 X = e[0], Y = e[1], Zt = e[2], W = BALL ? e[3] : Z4;
+            vote_pair_pk<STICK, PLATE, BALL>(Ap, Bp, lp, ubp, vbp, oxp, oy2, oz21, X, Y, Zt, W, P1);
+            vote_pair_pk<STICK, PLATE, BALL>(Am, Bm, lm, ubm, vbm, oxm, oy2, oz21, X, Y, Zt, W, P1);
+        }
+        e2 += step;
+        step += 2;
+        oxf += 1.0f;
+    }
+}
+
 template <bool STICK, bool PLATE, bool BALL>
 __global__ void __launch_bounds__(VX * VY, TVGB_FAST_MINB) k_vote3_pk(FastArgs a) {
     constexpr int R = 4;
@@ -642,6 +695,13 @@ __global__ void __launch_bounds__(VX * VY, TVGB_FAST_MINB) k_vote3_pk(FastArgs a
                 if ((unsigned)(y0 + int(threadIdx.y) + oy) >= (unsigned)s1) continue;   // warp-uniform
                 const int rr = threadIdx.y + (oy - oy0);
                 const int base = rr * SW + threadIdx.x + hw;
+#if TVGB_PK_FUSE
+                if (pv[0] && pv[1]) {
+                    vote_row_pk2<STICK, PLATE, BALL>(sA + base, sB + base, sC + base, ptab, ptab + size_t(ne) * NQ, NQ,
+                                                     oz2[0], oz2[1], float(oy), oy * oy, hw, P[0], P[1]);
+                    continue;
+                }
+#endif
 #pragma unroll
                 for (int p = 0; p < 2; ++p)
                     if (pv[p])
