@@ -317,6 +317,13 @@ int tvgb_memory_stats(unsigned long long* scratch_bytes, unsigned long long* scr
 int tvgb_profile_enable(int on);
 int tvgb_profile_read(char* buf, size_t buflen);
 
+/* Measured FP32 peak (no reference counterpart; the denominator of the
+ * voting kernels' roofline): a kernel of independent packed FP32 fused
+ * multiply-add chains on every SM for ~40 ms.  *tflops gets its rate (an FMA
+ * = 2 flops), *sm_mhz (may be NULL) the mean SM clock it ran at, from the
+ * SMs' cycle counters against the global timer. */
+int tvgb_fp32_peak(double* tflops, double* sm_mhz, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -70,6 +70,7 @@ SIGNATURES = {
     "tvgb_sticknorm3": (ctypes.c_double, [_F, _F, _U]),
     "tvgb_profile_enable": (_I, [_I]),
     "tvgb_profile_read": (_I, [ctypes.c_char_p, _SZ]),
+    "tvgb_fp32_peak": (_I, [_P, _P, _P]),
 }
 
 _lib = None

@@ -112,9 +112,71 @@ void scratch_track(long long delta) {
     }
 }
 
+// FP32 FMA throughput: every thread runs 8 independent chains of packed
+// FP32x2 fused multiply-adds (16 FMAs per iteration).  Each CTA records its
+// SM-clock cycles and its global-timer nanoseconds, so the host learns the SM
+// clock the kernel ran at.
+__global__ void __launch_bounds__(256) k_fp32_peak(int iters, float* __restrict__ sink,
+                                                   unsigned long long* __restrict__ clk) {
+    float2 a[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) a[i] = make_float2(1e-3f * float(threadIdx.x + i), 2e-3f * float(i));
+    const float2 m = make_float2(0.9999f, 0.9998f), c = make_float2(1e-6f, 2e-6f);
+    unsigned long long t0, t1;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+    const long long c0 = clock64();
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) a[i] = __ffma2_rn(a[i], m, c);
+    }
+    const long long c1 = clock64();
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t1));
+    float s = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) s += a[i].x + a[i].y;
+    if (s == 1234.5f) sink[0] = s;   // keeps the chains alive
+    if (threadIdx.x == 0) {
+        atomicAdd(clk, (unsigned long long)(c1 - c0));
+        atomicAdd(clk + 1, t1 - t0);
+    }
+}
+
 }  // namespace tvgb
 
 extern "C" {
+
+int tvgb_fp32_peak(double* tflops, double* sm_mhz, void* stream) {
+    using namespace tvgb;
+    TVGB_CHECK_ARG(tflops, "tvgb_fp32_peak: tflops is NULL");
+    cudaStream_t st = as_stream(stream);
+    int dev = 0, sms = 0;
+    TVGB_CUDA(cudaGetDevice(&dev));
+    TVGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int ctas = sms * 8, iters = 1 << 18;
+    Scratch scr;
+    TVGB_TRY(scr.alloc(64, st));
+    unsigned long long* clk = scr.get<unsigned long long>();
+    cudaEvent_t e0, e1;
+    TVGB_CUDA(cudaEventCreate(&e0));
+    TVGB_CUDA(cudaEventCreate(&e1));
+    k_fp32_peak<<<ctas, 256, 0, st>>>(iters / 8, reinterpret_cast<float*>(clk + 2), clk);   // warm-up
+    TVGB_CUDA(cudaMemsetAsync(clk, 0, 16, st));
+    TVGB_CUDA(cudaEventRecord(e0, st));
+    k_fp32_peak<<<ctas, 256, 0, st>>>(iters, reinterpret_cast<float*>(clk + 2), clk);
+    TVGB_CUDA(cudaEventRecord(e1, st));
+    TVGB_LAUNCHED();
+    unsigned long long h[2] = {0, 0};
+    TVGB_CUDA(cudaMemcpyAsync(h, clk, 16, cudaMemcpyDeviceToHost, st));
+    TVGB_CUDA(cudaStreamSynchronize(st));
+    float ms = 0.0f;
+    TVGB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    const double flops = 2.0 * 16.0 * double(iters) * double(ctas) * 256.0;
+    *tflops = flops / (double(ms) * 1e-3) / 1e12;
+    if (sm_mhz) *sm_mhz = h[1] ? 1e3 * double(h[0]) / double(h[1]) : 0.0;
+    return TVGB_OK;
+}
 
 const char* tvgb_last_error(void) { return tvgb::g_last_error; }
 int tvgb_version(void) { return 100; }

@@ -564,6 +564,10 @@ __device__ __forceinline__ void vote_row_pk(const float4* __restrict__ rA, const
 #ifndef TVGB_PK_FUSE
 #define TVGB_PK_FUSE 1         // both receiver pairs per voter-row pass
 #endif
+#ifndef TVGB_PK2_UNROLL
+#define TVGB_PK2_UNROLL 3      // unroll factor of that pass's +-ox loop
+#endif
+constexpr int kPk2Unroll = TVGB_PK2_UNROLL;
 template <bool STICK, bool PLATE, bool BALL>
 __device__ __forceinline__ void vote_row_pk2(const float4* __restrict__ rA, const float4* __restrict__ rB,
                                              const float* __restrict__ rC, const float4* __restrict__ pt0,
@@ -586,7 +590,7 @@ __device__ __forceinline__ void vote_row_pk2(const float4* __restrict__ rA, cons
     float oxf = 1.0f;
     int e2 = 1 + L2y;
     int step = 3;                        // (ox + 1)^2 - ox^2 for ox = 1
-#pragma unroll 1
+#pragma unroll kPk2Unroll
     for (int d = 1; d <= hw; ++d) {
         const float4 Ap = STICK ? rA[d] : Z4, Am = STICK ? rA[-d] : Z4;
         const float4 Bp = PLATE ? rB[d] : Z4, Bm = PLATE ? rB[-d] : Z4;
