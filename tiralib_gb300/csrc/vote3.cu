@@ -564,6 +564,9 @@ __device__ __forceinline__ void vote_row_pk(const float4* __restrict__ rA, const
 #ifndef TVGB_PK_FUSE
 #define TVGB_PK_FUSE 1         // both receiver pairs per voter-row pass
 #endif
+#ifndef TVGB_PK_BALL
+#define TVGB_PK_BALL 1         // the packed kernel also for votes with the ball term
+#endif
 #ifndef TVGB_PK2_UNROLL
 #define TVGB_PK2_UNROLL 3      // unroll factor of that pass's +-ox loop
 #endif
@@ -994,7 +997,7 @@ static int launch_fast(FastArgs a, bool S, bool P, bool B, cudaStream_t st) {
     // rows per stage: the largest count that keeps TVGB_FAST_MINB CTAs per SM
     const int w = 2 * a.hw + 1;
     const size_t budget = (TVGB_FAST_MINB >= 3 ? 72 : 100) * 1024;
-    if (TVGB_PACKED && FAST_R == 4 && !B) {
+    if (TVGB_PACKED && FAST_R == 4 && (TVGB_PK_BALL || !B)) {
         int rows = w;
         while (rows > 1 && pk_smem(a.hw, rows, S, P, B) > budget) rows = (rows + 1) / 2;
         const size_t smem = pk_smem(a.hw, rows, S, P, B);
