@@ -11,10 +11,13 @@
  * bfloat16 (round to nearest even of the float32 value), as the tensor-core
  * inference computes; the backward pass treats the rounding as identity.
  * quant == 1: GELU exact, then rounded to bfloat16 (the GPU's FP32 GELU);
- * quant == 2: GELU in packed BF16 arithmetic as the GPU's training forward
- * pass and its tcgen05 inference compute it (every product or fused
- * multiply-add rounded to bfloat16 once, tanh exact then rounded; the
- * hardware's tanh approximation may differ from that in the last bit). */
+ * quant == 2: the activation as the GPU's training forward pass and its
+ * tcgen05 inference compute it: for units j with j % 8 < 6 the GELU in packed
+ * BF16 arithmetic (every product or fused multiply-add rounded to bfloat16
+ * once, tanh exact then rounded; the hardware's tanh approximation may differ
+ * from that in the last bit), for j % 8 >= 6 z * phi(z) with phi a clamped
+ * odd polynomial evaluated in float32 (exactly as the GPU does), rounded to
+ * bfloat16. */
 #include <math.h>
 #include <stdint.h>
 #include <string.h>
@@ -50,7 +53,20 @@ static double gelu_bf16(double z) {
     const double h = bf16r(zb * 0.5);
     return bf16r(h * t + h);
 }
-static double act(double z, int quant) { return quant == 2 ? gelu_bf16(z) : (quant ? bf16r(gelu(z)) : gelu(z)); }
+static double gelu_poly(double zd) {
+    const float z = (float)zd;
+    const float h = fminf(fmaxf(z, -3.0f), 3.0f);
+    const float s = h * h;
+    float p = fmaf(s, -0.000222746943f, 0.00561482186f);
+    p = fmaf(p, s, -0.0578609677f);
+    p = fmaf(p, s, 0.394045958f);
+    const float phi = fmaf(h, p, 0.5f);
+    return bf16r((double)(z * phi));
+}
+static double act(double z, int quant, int unit) {
+    if (quant == 2) return (unit & 7) >= 6 ? gelu_poly(z) : gelu_bf16(z);
+    return quant ? bf16r(gelu(z)) : gelu(z);
+}
 static double gelu_d(double z) {
     const double t = tanh(GELU_K * (z + GELU_A * z * z * z));
     return 0.5 * (1.0 + t) + 0.5 * z * (1.0 - t * t) * GELU_K * (1.0 + 3.0 * GELU_A * z * z);
@@ -96,19 +112,19 @@ double or_mlp_loss_grad(const double* P, const double* X, const double* T, int B
             double a = b1[j];
             for (int k = 0; k < MLP_IN; ++k) a += W1q[j * MLP_IN + k] * h0[k];
             z1[j] = a;
-            h1[j] = act(a, quant);
+            h1[j] = act(a, quant, j);
         }
         for (int j = 0; j < MLP_H; ++j) {
             double a = b2[j];
             for (int k = 0; k < MLP_H; ++k) a += W2q[j * MLP_H + k] * h1[k];
             z2[j] = a;
-            h2[j] = act(a, quant);
+            h2[j] = act(a, quant, j);
         }
         for (int j = 0; j < MLP_H; ++j) {
             double a = b3[j];
             for (int k = 0; k < MLP_H; ++k) a += W3q[j * MLP_H + k] * h2[k];
             z3[j] = a;
-            h3[j] = act(a, quant);
+            h3[j] = act(a, quant, j);
         }
         double dy[MLP_OUT];
         for (int o = 0; o < MLP_OUT; ++o) {

@@ -21,9 +21,11 @@
 // along N):  B1 64 x 16 at 0, B2 64 x 80 at 2048, B3 64 x 80 at 12288,
 // B4 16 x 80 at 22528; 25088 bytes in all.
 //
-// Where the time goes (GB300, measured per 128-row tile): the three GELU
-// epilogues (64 tanh per row each) on the MUFU pipe; with 4 CTAs per SM the
-// MMAs and their waits are hidden behind the other CTAs' epilogues.
+// Where the time goes (GB300, measured): the three GELU epilogues per tile.
+// With every unit on the tanh form the MUFU pipe was 71% busy; with one unit
+// in four on the FMA-pipe polynomial form the kernel is held by the chain of
+// four dependent MMA rounds per tile (about 80 cycles to issue each
+// tcgen05.mma), with only 4 tiles in flight per SM (512 TMEM columns).
 #pragma once
 #include "surrogate_mlp.cuh"
 #include "tc_sm100.cuh"
@@ -43,8 +45,9 @@ constexpr int TC_SMEM_PER_CTA = 52 * 1024;
 // = z0).  Mode 0: FP32 arithmetic with the hardware tanh, rounded once.
 // Mode 1: packed BF16 arithmetic, one MUFU operation per pair:
 //   zb = bf16(z); u = zb (K + K A zb^2); h = zb / 2; gelu = h + h tanh(u),
-// every product and fused multiply-add rounded to BF16 once.  Mode 1 is the
-// arithmetic of the training forward pass and of the surrogate vote.
+// every product and fused multiply-add rounded to BF16 once.  Mode 1, with
+// the polynomial form below on one unit in four, is the activation of the
+// training forward pass and of the surrogate vote.
 template <int GM>
 __device__ __forceinline__ uint32_t gelu_pair(float z0, float z1) {
     if (GM == 0) return pack_bf16x2(gelu_fast(z0), gelu_fast(z1));
@@ -58,6 +61,37 @@ __device__ __forceinline__ uint32_t gelu_pair(float z0, float z1) {
     const __nv_bfloat162 h = __hmul2(zb, half);
     const __nv_bfloat162 g = __hfma2(h, t, h);
     return *reinterpret_cast<const uint32_t*>(&g);
+}
+
+// The polynomial form of the GELU, for one unit in four (the units 8 u + 6 and
+// 8 u + 7): z * phi(z), phi the normal CDF as a clamped odd polynomial
+//   phi(z) = 1/2 + h (A1 + A3 s + A5 s^2 + A7 s^3),  h = clamp(z, -3, 3), s = h^2,
+// a weighted least-squares fit on [-3, 3] (max deviation 1.5e-3 from the
+// normal CDF), in FP32 arithmetic, rounded once to BF16.  It runs on the FMA
+// pipe while the other units' tanh occupy the MUFU pipe: with three units in
+// four on the MUFU the two pipes finish together.
+constexpr float GELU_PC = 3.0f;
+constexpr float GELU_P1 = 0.394045958f, GELU_P3 = -0.0578609677f, GELU_P5 = 0.00561482186f,
+                GELU_P7 = -0.000222746943f;
+__host__ __device__ constexpr bool gelu_is_poly(int col) { return (col & 7) >= 6; }
+
+__device__ __forceinline__ uint32_t gelu_poly_pair(float z0, float z1) {
+    const float2 z = make_float2(z0, z1);
+    const float2 h = make_float2(fminf(fmaxf(z0, -GELU_PC), GELU_PC), fminf(fmaxf(z1, -GELU_PC), GELU_PC));
+    const float2 s = __fmul2_rn(h, h);
+    float2 p = __ffma2_rn(s, make_float2(GELU_P7, GELU_P7), make_float2(GELU_P5, GELU_P5));
+    p = __ffma2_rn(p, s, make_float2(GELU_P3, GELU_P3));
+    p = __ffma2_rn(p, s, make_float2(GELU_P1, GELU_P1));
+    const float2 phi = __ffma2_rn(h, p, make_float2(0.5f, 0.5f));
+    const float2 g = __fmul2_rn(z, phi);
+    return pack_bf16x2(g.x, g.y);
+}
+
+// the activation of the unit pair (col, col + 1) or, in training, of two
+// units of the same kind: the polynomial form for gelu_is_poly units, the
+// packed-BF16 tanh form otherwise
+__device__ __forceinline__ uint32_t gelu_unit_pair(float z0, float z1, bool poly) {
+    return poly ? gelu_poly_pair(z0, z1) : gelu_pair<1>(z0, z1);
 }
 
 // this thread's TMEM lane quarter (warp w owns lanes 32 (w % 4) ..)
@@ -136,8 +170,10 @@ __device__ __forceinline__ void sur_tc_hidden(const SurTc& s) {
         uint32_t r[32];
         tc::tmem_ld32(t + TC_D + 32 * h, r);
 #pragma unroll
-        for (int i = 0; i < 16; ++i)
-            act[16 * h + i] = gelu_pair<GM>(__uint_as_float(r[2 * i]), __uint_as_float(r[2 * i + 1]));
+        for (int i = 0; i < 16; ++i) {
+            const float z0 = __uint_as_float(r[2 * i]), z1 = __uint_as_float(r[2 * i + 1]);
+            act[16 * h + i] = GM == 1 ? gelu_unit_pair(z0, z1, gelu_is_poly(32 * h + 2 * i)) : gelu_pair<0>(z0, z1);
+        }
     }
     tc::tmem_st32(t + TC_A, act);
 }

@@ -230,8 +230,8 @@ __global__ void __launch_bounds__(256) k_sur_fwd_bwd(const float* __restrict__ P
                 a1 = fmaf(wt[k * TRS + lane + 32], x, a1);
             }
             z[s * SUR_H + lane] = a0; z[s * SUR_H + lane + 32] = a1;
-            // the inference's GELU (packed BF16 arithmetic), elementwise on the pair
-            const uint32_t g2 = gelu_pair<1>(a0, a1);
+            // the inference's activation of units lane and lane + 32 (the same kind)
+            const uint32_t g2 = gelu_unit_pair(a0, a1, gelu_is_poly(lane));
             h[s * SUR_H + lane] = __uint_as_float(g2 << 16);
             h[s * SUR_H + lane + 32] = __uint_as_float(g2 & 0xffff0000u);
         }
