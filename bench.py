@@ -506,6 +506,8 @@ def surrogate_study(vol_d, cfg, args, dev):
         kms[key] = ms / max(nl, 1)
         res[key] = o.cpu().numpy().reshape(-1, 9)[:, [0, 1, 2, 4, 5, 8]].astype(np.float64)
         stats[key] = st
+    rates = (ctypes.c_double * 4)()
+    lib.tvgb_pipe_rates(rates, None)
     ex = res["closed"]
     nex = np.linalg.norm(ex)
     err = {k: {"normwise": float(np.linalg.norm(v - ex) / nex), "max_abs_over_max": float(np.abs(v - ex).max() /
@@ -526,6 +528,8 @@ def surrogate_study(vol_d, cfg, args, dev):
         "rel_err_vs_exact": err,
         "judge": {"tol": 1e-3, "ctas": int(stats["surrogate_judged"][0]),
                   "recomputed_exactly": int(stats["surrogate_judged"][1])},
+        "pipe_rates_per_sm_clock": {"fp32_fma": rates[0], "tanh_f32": rates[1], "tanh_bf16x2_results": rates[2],
+                                    "sm_mhz": rates[3]},
     }
 
 

@@ -324,6 +324,12 @@ int tvgb_profile_read(char* buf, size_t buflen);
  * SMs' cycle counters against the global timer. */
 int tvgb_fp32_peak(double* tflops, double* sm_mhz, void* stream);
 
+/* Measured pipe rates per SM clock (no reference counterpart; they bound the
+ * learned vote's activations): rates[0] FP32 FMAs, rates[1] tanh.approx.f32
+ * results, rates[2] tanh.approx.bf16x2 results (two per instruction),
+ * rates[3] the SM clock in MHz, all from throughput kernels on every SM. */
+int tvgb_pipe_rates(double* rates, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

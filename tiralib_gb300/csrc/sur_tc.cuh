@@ -24,8 +24,8 @@
 // Where the time goes (GB300, measured): the three GELU epilogues per tile.
 // With every unit on the tanh form the MUFU pipe was 71% busy; with one unit
 // in four on the FMA-pipe polynomial form the kernel is held by the chain of
-// four dependent MMA rounds per tile (about 80 cycles to issue each
-// tcgen05.mma), with only 4 tiles in flight per SM (512 TMEM columns).
+// four dependent MMA rounds per tile, with only 4 tiles in flight per SM
+// (512 TMEM columns).
 #pragma once
 #include "surrogate_mlp.cuh"
 #include "tc_sm100.cuh"

@@ -141,9 +141,72 @@ __global__ void __launch_bounds__(256) k_fp32_peak(int iters, float* __restrict_
     }
 }
 
+// MUFU throughput: 8 independent chains of tanh.approx per thread, FP32
+// (MODE 0) or packed BF16 pairs (MODE 1).
+template <int MODE>
+__global__ void __launch_bounds__(256) k_tanh_rate(int iters, float* __restrict__ sink) {
+    float a[8];
+    uint32_t b[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        a[i] = 1e-3f * float(threadIdx.x + i);
+        b[i] = 0x3C003C00u + uint32_t(i);
+    }
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            if (MODE == 0) asm volatile("tanh.approx.f32 %0, %0;" : "+f"(a[i]));
+            else asm volatile("tanh.approx.bf16x2 %0, %0;" : "+r"(b[i]));
+        }
+    }
+    float s = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) s += a[i] + __uint_as_float(b[i]);
+    if (s == 1234.5f) sink[0] = s;
+}
+
 }  // namespace tvgb
 
 extern "C" {
+
+int tvgb_pipe_rates(double* rates, void* stream) {
+    using namespace tvgb;
+    TVGB_CHECK_ARG(rates, "tvgb_pipe_rates: rates is NULL");
+    double tf = 0.0, mhz = 0.0;
+    TVGB_TRY(tvgb_fp32_peak(&tf, &mhz, stream));
+    TVGB_CHECK_ARG(mhz > 0.0, "tvgb_pipe_rates: the SM clock could not be measured");
+    cudaStream_t st = as_stream(stream);
+    int dev = 0, sms = 0;
+    TVGB_CUDA(cudaGetDevice(&dev));
+    TVGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int ctas = sms * 8, iters = 1 << 13;
+    Scratch scr;
+    TVGB_TRY(scr.alloc(16, st));
+    cudaEvent_t e0, e1;
+    TVGB_CUDA(cudaEventCreate(&e0));
+    TVGB_CUDA(cudaEventCreate(&e1));
+    rates[0] = tf * 1e12 / 2.0 / (double(sms) * mhz * 1e6);   // FP32 FMAs per SM clock
+    for (int mode = 0; mode < 2; ++mode) {
+        auto launch = [&](int n) {
+            if (mode == 0) k_tanh_rate<0><<<ctas, 256, 0, st>>>(n, scr.get<float>());
+            else k_tanh_rate<1><<<ctas, 256, 0, st>>>(n, scr.get<float>());
+        };
+        launch(iters / 8);   // warm-up
+        TVGB_CUDA(cudaEventRecord(e0, st));
+        launch(iters);
+        TVGB_CUDA(cudaEventRecord(e1, st));
+        TVGB_LAUNCHED();
+        TVGB_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.0f;
+        TVGB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        const double results = double(ctas) * 256.0 * iters * 8.0 * (mode == 1 ? 2.0 : 1.0);
+        rates[1 + mode] = results / (double(ms) * 1e-3) / (double(sms) * mhz * 1e6);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    rates[3] = mhz;
+    return TVGB_OK;
+}
 
 int tvgb_fp32_peak(double* tflops, double* sm_mhz, void* stream) {
     using namespace tvgb;
