@@ -309,6 +309,11 @@ unsigned long long tvgb_launch_count(void);
  * value after reading it. */
 int tvgb_memory_stats(unsigned long long* scratch_bytes, unsigned long long* scratch_peak_bytes, int reset_peak);
 
+/* Device memory the library has freed stays in its own per-device pool for
+ * the next call (no reference counterpart: the reference allocates and frees
+ * per call).  This returns every pool's unused memory to the driver. */
+int tvgb_release_cached_memory(void);
+
 /* Opt-in per-kernel timing (no reference counterpart; the reference has no
  * timers): while enabled, every launch is bracketed by a CUDA event pair on
  * its stream.  tvgb_profile_read resolves the recorded launches (waiting on

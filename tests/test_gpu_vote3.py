@@ -165,3 +165,22 @@ def test_vote3_rejects_bad_arguments(tv):
     out = np.zeros_like(T)
     with pytest.raises(tv.TvgbError):
         tv.tensorvote3(T, out, 4, 4, 4, 1.0, 0.0, 6, 1)
+
+
+def test_repeated_host_calls_reuse_the_library_pool():
+    """Host-array calls stage through the library's own memory pool, which
+    keeps freed memory for the next call; results are unchanged from call to
+    call, the library's live temporaries return to zero, and the cached
+    memory can be handed back to the driver."""
+    import tiralib_gb300 as tv
+    rng = np.random.default_rng(5)
+    A = rng.normal(size=(18, 20, 22, 3, 3))
+    T = (A @ np.swapaxes(A, -1, -2)).astype(np.float32)
+    first, ev1, _ = tv.vote3(T, 2.0, 0.0, w=9, evals=True)
+    again, ev2, _ = tv.vote3(T, 2.0, 0.0, w=9, evals=True)
+    np.testing.assert_array_equal(first, again)
+    np.testing.assert_array_equal(ev1, ev2)
+    assert tv.memory_stats()[0] == 0
+    assert tv.lib().tvgb_release_cached_memory() == 0
+    third, _, _ = tv.vote3(T, 2.0, 0.0, w=9)
+    np.testing.assert_array_equal(first, third)

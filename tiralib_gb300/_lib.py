@@ -71,6 +71,7 @@ SIGNATURES = {
     "tvgb_profile_enable": (_I, [_I]),
     "tvgb_profile_read": (_I, [ctypes.c_char_p, _SZ]),
     "tvgb_fp32_peak": (_I, [_P, _P, _P]),
+    "tvgb_release_cached_memory": (_I, []),
     "tvgb_pipe_rates": (_I, [_P, _P]),
 }
 

@@ -54,6 +54,48 @@ bool is_device_ptr(const void* p) {
     return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
+// The library's stream-ordered allocations come from its own memory pool,
+// one per device, which keeps freed memory for the next call (release
+// threshold at the maximum).  The device's default pool returns freed memory
+// to the driver at every synchronisation, and mapping it again cost ~20 ms per
+// call of the 3D pipeline on host arrays.  tvgb_release_cached_memory trims
+// the pools.
+constexpr int kMaxPoolDevices = 64;
+static std::mutex g_pool_mu;
+static cudaMemPool_t g_pools[kMaxPoolDevices];
+
+static int device_pool(cudaMemPool_t& pool) {
+    int dev = 0;
+    TVGB_CUDA(cudaGetDevice(&dev));
+    TVGB_CHECK_ARG(dev >= 0 && dev < kMaxPoolDevices, "device %d beyond the library's pool table", dev);
+    std::lock_guard<std::mutex> g(g_pool_mu);
+    if (!g_pools[dev]) {
+        cudaMemPoolProps props{};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        cudaMemPool_t p = nullptr;
+        TVGB_CUDA(cudaMemPoolCreate(&p, &props));
+        unsigned long long keep = ~0ull;   // the attribute is a 64-bit value
+        const cudaError_t e = cudaMemPoolSetAttribute(p, cudaMemPoolAttrReleaseThreshold, &keep);
+        if (e != cudaSuccess) {
+            cudaMemPoolDestroy(p);
+            set_error("cudaMemPoolSetAttribute failed: %s", cudaGetErrorString(e));
+            return TVGB_ERR_CUDA;
+        }
+        g_pools[dev] = p;
+    }
+    pool = g_pools[dev];
+    return TVGB_OK;
+}
+
+static int pool_alloc(void** ptr, size_t bytes, cudaStream_t s) {
+    cudaMemPool_t pool;
+    TVGB_TRY(device_pool(pool));
+    TVGB_CUDA(cudaMallocFromPoolAsync(ptr, bytes, pool, s));
+    return TVGB_OK;
+}
+
 int DevArray::in(const void* p, size_t nbytes, cudaStream_t s) {
     user = const_cast<void*>(p);
     bytes = nbytes;
@@ -64,7 +106,7 @@ int DevArray::in(const void* p, size_t nbytes, cudaStream_t s) {
         dev = user;
         return TVGB_OK;
     }
-    TVGB_CUDA(cudaMallocAsync(&dev, nbytes, s));
+    TVGB_TRY(pool_alloc(&dev, nbytes, s));
     owned = true;
     scratch_track((long long)nbytes);
     TVGB_CUDA(cudaMemcpyAsync(dev, p, nbytes, cudaMemcpyHostToDevice, s));
@@ -80,7 +122,7 @@ int DevArray::out(void* p, size_t nbytes, cudaStream_t s, bool zero) {
     if (is_device_ptr(p)) {
         dev = p;
     } else {
-        TVGB_CUDA(cudaMallocAsync(&dev, nbytes, s));
+        TVGB_TRY(pool_alloc(&dev, nbytes, s));
         owned = true;
         scratch_track((long long)nbytes);
     }
@@ -97,7 +139,7 @@ int DevArray::finish() {
 int Scratch::alloc(size_t bytes, cudaStream_t s) {
     stream = s;
     if (bytes == 0) return TVGB_OK;
-    TVGB_CUDA(cudaMallocAsync(&p, bytes, s));
+    TVGB_TRY(pool_alloc(&p, bytes, s));
     this->bytes = bytes;
     scratch_track((long long)bytes);
     return TVGB_OK;
@@ -250,6 +292,16 @@ int tvgb_memory_stats(unsigned long long* scratch_bytes, unsigned long long* scr
     if (scratch_bytes) *scratch_bytes = (unsigned long long)(cur > 0 ? cur : 0);
     if (scratch_peak_bytes) *scratch_peak_bytes = (unsigned long long)tvgb::g_scratch_peak.load();
     if (reset_peak) tvgb::g_scratch_peak.store(cur > 0 ? cur : 0);
+    return TVGB_OK;
+}
+
+int tvgb_release_cached_memory(void) {
+    std::lock_guard<std::mutex> g(tvgb::g_pool_mu);
+    for (int d = 0; d < tvgb::kMaxPoolDevices; ++d)
+        if (tvgb::g_pools[d] && cudaMemPoolTrimTo(tvgb::g_pools[d], 0) != cudaSuccess) {
+            tvgb::set_error("cudaMemPoolTrimTo failed on device %d", d);
+            return TVGB_ERR_CUDA;
+        }
     return TVGB_OK;
 }
 
