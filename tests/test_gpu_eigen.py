@@ -157,3 +157,28 @@ def test_eig2_matches_reference(tv, golden):
     d = np.abs(th - g["evecs2"])
     d = np.minimum(d, np.abs(d - 2 * np.pi))
     assert d.max() < 1e-4
+
+
+@pytest.mark.parametrize("precise", [False, True])
+def test_eig3_streamed_host_batch_equals_device_batch(tv, precise):
+    """A large batch in host memory runs chunk by chunk, its copies
+    overlapped with the solve on a ring of streams; the results and the
+    refined count equal those of the same batch solved in device memory
+    (the last chunk is ragged)."""
+    import torch
+    rng = np.random.default_rng(11)
+    n = (1 << 23) + 12345
+    Q, _ = np.linalg.qr(rng.normal(size=(4096, 3, 3)))
+    lam = rng.uniform(-2, 2, size=(4096, 3))
+    lam[::7, 1] = lam[::7, 0] * (1 + 1e-6)          # near-degenerate pairs
+    base = (Q * lam[:, None, :]) @ np.swapaxes(Q, 1, 2)
+    M = base[rng.integers(0, 4096, size=n)].astype(np.float32).reshape(n, 9)
+    M += rng.normal(scale=1e-3, size=(n, 1)).astype(np.float32) * np.eye(3, dtype=np.float32).reshape(1, 9)
+    ev_h, vec_h, nr_h = tv.eig3(M, layout="mat3", evecs="cartesian", precise=precise)
+    Md = torch.from_numpy(M).cuda()
+    ev_d, vec_d, nr_d = tv.eig3(Md, layout="mat3", evecs="cartesian", precise=precise)
+    np.testing.assert_array_equal(ev_h, ev_d.cpu().numpy())
+    np.testing.assert_array_equal(vec_h, vec_d.cpu().numpy())
+    assert nr_h == nr_d
+    if precise:
+        assert nr_h > 0

@@ -275,6 +275,72 @@ using namespace tvgb;
 
 extern "C" {
 
+// Host arrays in, host arrays out: the batch is cut into chunks that flow
+// through a ring of device buffers on their own streams, so the host->device
+// copy of one chunk, the solve of another and the device->host copy of a
+// third run at the same time (separate copy engines each way).  Ordered after
+// the caller's stream's earlier work, and the caller's stream after the last
+// chunk.
+static int eig3_streamed(const float* mats, int in_layout, size_t n, float* evals3, float* evecs, int fmt,
+                         bool precise, unsigned long long* nref, cudaStream_t s) {
+    constexpr size_t CH = size_t(1) << 22;
+    constexpr int NB = 3;
+    const size_t nf = in_layout == TVGB_LAYOUT_MAT3 ? 9 : 6;
+    const size_t nv = fmt == 1 ? 9 : (fmt == 2 ? 6 : 0);
+    const size_t per = CH * (nf + 3 + nv);
+    Scratch buf;
+    TVGB_TRY(buf.alloc(NB * per * sizeof(float), s));
+    cudaStream_t ss[NB] = {};
+    cudaEvent_t fork = nullptr, join[NB] = {};
+    int rc = TVGB_OK;
+    auto cuda = [&](cudaError_t e, const char* what) {
+        if (e != cudaSuccess && rc == TVGB_OK) {
+            set_error("tvgb_eig3 (streamed): %s failed: %s", what, cudaGetErrorString(e));
+            rc = TVGB_ERR_CUDA;
+        }
+        return e == cudaSuccess;
+    };
+    bool ok = cuda(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming), "cudaEventCreate");
+    for (int b = 0; ok && b < NB; ++b)
+        ok = cuda(cudaStreamCreateWithFlags(&ss[b], cudaStreamNonBlocking), "cudaStreamCreate") &&
+             cuda(cudaEventCreateWithFlags(&join[b], cudaEventDisableTiming), "cudaEventCreate");
+    ok = ok && cuda(cudaEventRecord(fork, s), "cudaEventRecord");
+    for (int b = 0; ok && b < NB; ++b) ok = cuda(cudaStreamWaitEvent(ss[b], fork, 0), "cudaStreamWaitEvent");
+    size_t i = 0;
+    for (size_t c = 0; ok && c < n; c += CH, ++i) {
+        const int b = int(i % NB);
+        const size_t m = n - c < CH ? n - c : CH;
+        float* din = buf.get<float>() + b * per;
+        float* dev = din + CH * nf;
+        float* dvec = dev + CH * 3;
+        ok = cuda(cudaMemcpyAsync(din, mats + c * nf, m * nf * sizeof(float), cudaMemcpyHostToDevice, ss[b]),
+                  "cudaMemcpyAsync");
+        if (ok) {
+            const int r = eig3_device(din, in_layout, m, dev, nv ? dvec : nullptr, fmt, precise, nref, ss[b]);
+            if (r != TVGB_OK) {
+                rc = r;
+                ok = false;
+            }
+        }
+        ok = ok && cuda(cudaMemcpyAsync(evals3 + c * 3, dev, m * 3 * sizeof(float), cudaMemcpyDeviceToHost, ss[b]),
+                        "cudaMemcpyAsync");
+        if (ok && nv)
+            ok = cuda(cudaMemcpyAsync(evecs + c * nv, dvec, m * nv * sizeof(float), cudaMemcpyDeviceToHost, ss[b]),
+                      "cudaMemcpyAsync");
+    }
+    // join every stream that was created, also after a failure, before the buffers are released on s
+    for (int b = 0; b < NB; ++b) {
+        if (ss[b] && join[b] && cudaEventRecord(join[b], ss[b]) == cudaSuccess) cudaStreamWaitEvent(s, join[b], 0);
+        else if (ss[b]) cudaStreamSynchronize(ss[b]);
+    }
+    for (int b = 0; b < NB; ++b) {
+        if (join[b]) cudaEventDestroy(join[b]);
+        if (ss[b]) cudaStreamDestroy(ss[b]);
+    }
+    if (fork) cudaEventDestroy(fork);
+    return rc;
+}
+
 int tvgb_eig3(const float* mats, int in_layout, size_t n, float* evals3, float* evecs, int evec_format, int mode,
               size_t* n_refined, void* stream) {
     TVGB_CHECK_ARG(mats || n == 0, "tvgb_eig3: mats is NULL");
@@ -287,15 +353,28 @@ int tvgb_eig3(const float* mats, int in_layout, size_t n, float* evals3, float* 
     cudaStream_t s = as_stream(stream);
     const size_t nf = in_layout == TVGB_LAYOUT_MAT3 ? 9 : 6;
     const size_t nv = evec_format == 1 ? 9 : (evec_format == 2 ? 6 : 0);
-    DevArray din, dev_, dvec;
-    TVGB_TRY(din.in(mats, n * nf * sizeof(float), s));
-    TVGB_TRY(dev_.out(evals3, n * 3 * sizeof(float), s));
-    TVGB_TRY(dvec.out(nv ? evecs : nullptr, n * nv * sizeof(float), s));
     Scratch cnt;
     if (n_refined && mode == TVGB_EIG_PRECISE) {
         TVGB_TRY(cnt.alloc(sizeof(unsigned long long), s));
         TVGB_CUDA(cudaMemsetAsync(cnt.p, 0, sizeof(unsigned long long), s));
     }
+    // large batches wholly in host memory (interleaved layouts): copies overlapped with the solve
+    if (n >= (size_t(1) << 23) && in_layout != TVGB_LAYOUT_SYM6_PLANES && evals3 && !is_device_ptr(mats) &&
+        !is_device_ptr(evals3) && (!nv || (evecs && !is_device_ptr(evecs)))) {
+        TVGB_TRY(eig3_streamed(mats, in_layout, n, evals3, evecs, evec_format, mode == TVGB_EIG_PRECISE,
+                               cnt.get<unsigned long long>(), s));
+        if (cnt.p) {
+            unsigned long long h = 0;
+            TVGB_CUDA(cudaMemcpyAsync(&h, cnt.p, sizeof(h), cudaMemcpyDeviceToHost, s));
+            *n_refined = size_t(h);
+        }
+        TVGB_CUDA(cudaStreamSynchronize(s));
+        return TVGB_OK;
+    }
+    DevArray din, dev_, dvec;
+    TVGB_TRY(din.in(mats, n * nf * sizeof(float), s));
+    TVGB_TRY(dev_.out(evals3, n * 3 * sizeof(float), s));
+    TVGB_TRY(dvec.out(nv ? evecs : nullptr, n * nv * sizeof(float), s));
     TVGB_TRY(eig3_device(din.get<float>(), in_layout, n, dev_.get<float>(), dvec.get<float>(), evec_format,
                          mode == TVGB_EIG_PRECISE, cnt.get<unsigned long long>(), s));
     TVGB_TRY(dev_.finish());
