@@ -18,6 +18,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
+#include <mutex>
 #include <vector>
 
 namespace tvgb {
@@ -263,27 +264,82 @@ __global__ void __launch_bounds__(V2X * V2Y) k_vote2_atv(const float4* __restric
     out[size_t(y) * s1 + x] = make_float4(oa, ob, ob, oc);
 }
 
+// Tables the library builds itself stay on the device, one per (device,
+// window, sigmas, power, samples, terms), so a repeated vote neither copies
+// nor waits for its table.  At most kTableCache tables are kept (a parameter
+// sweep beyond that builds and uploads the extra ones per call).
+struct TableEntry {
+    int dev, w, power, samples, stick, plate, nbc, h;
+    float s1, s2;
+    Nb2* table;
+};
+constexpr int kTableCache = 128;
+static std::mutex g_tab_mu;
+static std::vector<TableEntry> g_tabs;
+
+static int cached_table(int w, float s1, float s2, unsigned power, unsigned samples, bool stick, bool plate,
+                        const TableEntry*& hit) {
+    hit = nullptr;
+    int dev = 0;
+    TVGB_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> g(g_tab_mu);
+    for (const TableEntry& e : g_tabs)
+        if (e.dev == dev && e.w == w && e.s1 == s1 && e.s2 == s2 && e.power == int(power) &&
+            e.samples == int(samples) && e.stick == int(stick) && e.plate == int(plate)) {
+            hit = &e;
+            return TVGB_OK;
+        }
+    if (int(g_tabs.size()) >= kTableCache) return TVGB_OK;
+    std::vector<Nb2> t(size_t(w) * w);
+    const int nbc = build_table(w, s1, s2, power, samples, stick, plate, t.data());
+    int h = 0;
+    for (int i = 0; i < nbc; ++i) h = std::max(h, std::max(std::abs(t[i].du), std::abs(t[i].dv)));
+    Nb2* d = nullptr;
+    if (nbc > 0) {
+        TVGB_CUDA(cudaMalloc(&d, size_t(nbc) * sizeof(Nb2)));
+        const cudaError_t e = cudaMemcpy(d, t.data(), size_t(nbc) * sizeof(Nb2), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            cudaFree(d);
+            set_error("table upload failed: %s", cudaGetErrorString(e));
+            return TVGB_ERR_CUDA;
+        }
+    }
+    g_tabs.reserve(kTableCache);   // entries never move: hit stays valid
+    g_tabs.push_back(TableEntry{dev, w, int(power), int(samples), int(stick), int(plate), nbc, h, s1, s2, d});
+    hit = &g_tabs.back();
+    return TVGB_OK;
+}
+
 // One TK vote of prepared voter records V (k_prep2) into out: the
-// Neighbor2D table is the caller's (host or device) or built here with the
-// reference's float steps; the staged kernel runs whenever the table is on
-// the host and its voter tile fits in shared memory.
+// Neighbor2D table is the caller's (host or device) or the library's own
+// (cached on the device); the staged kernel runs whenever the table's extent
+// is known and its voter tile fits in shared memory.
 static int vote2_tk_launch(const float4* V, const Nb2* host_or_dev_nb, int nbc, float s1, float s2, int power,
                            unsigned w, unsigned S0, unsigned S1, bool stick, bool plate, unsigned samples, float4* out,
                            cudaStream_t st) {
     const bool use_plate = plate && samples > 0;
     std::vector<Nb2> table;
     const Nb2* nbp = host_or_dev_nb;
+    const TableEntry* cached = nullptr;
     if (!nbp) {
-        table.resize(size_t(w) * w);
-        nbc = build_table(int(w), s1, s2, unsigned(power), samples, stick, use_plate, table.data());
-        nbp = table.data();
+        TVGB_TRY(cached_table(int(w), s1, s2, unsigned(power), samples, stick, use_plate, cached));
+        if (cached) {
+            nbp = cached->table;
+            nbc = cached->nbc;
+        } else {
+            table.resize(size_t(w) * w);
+            nbc = build_table(int(w), s1, s2, unsigned(power), samples, stick, use_plate, table.data());
+            nbp = table.data();
+        }
     }
     DevArray dnb;
     TVGB_TRY(dnb.in(nbp, size_t(nbc) * sizeof(Nb2), st));
     const unsigned p = power < 1 ? 1u : unsigned(power);
     const float eta_s = stick_norm_2d_h(s1, s2, p);
     int h = -1;
-    if (!is_device_ptr(nbp)) {
+    if (cached) {
+        h = cached->h;
+    } else if (!is_device_ptr(nbp)) {
         h = 0;
         for (int i = 0; i < nbc; ++i) h = std::max(h, std::max(std::abs(nbp[i].du), std::abs(nbp[i].dv)));
     }
@@ -333,7 +389,7 @@ static int vote2_tk_launch(const float4* V, const Nb2* host_or_dev_nb, int nbc, 
         kt_.stop();
     }
     TVGB_LAUNCHED();
-    if (!host_or_dev_nb) TVGB_CUDA(cudaStreamSynchronize(st));   // the host table must outlive its copy
+    if (!host_or_dev_nb && !cached) TVGB_CUDA(cudaStreamSynchronize(st));   // the host table must outlive its copy
     return TVGB_OK;
 }
 
