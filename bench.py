@@ -1,13 +1,14 @@
 #!/usr/bin/env python
 """Benchmark of the tensor-voting path on one GB300 per process.
 
-Workload (default, --config c2): a seeded synthetic 256^3 float32 volume of
-64 tubes (radius 1-3 voxels, 8-segment piecewise-linear centrelines) plus
-N(0, 0.05) noise -> 3x3 structure tensor (gradient, outer product, separable
-Gaussian sigma 1.5, 9 taps, same-size output) -> TK stick + plate voting at
-sigma 4 (w = 25, samples = 20; the plate is the exact orientation integral)
--> per-voxel 3x3 eigendecomposition of the voted field.  One "step" is that
-whole pass over the volume; the metric is voxels per second.
+Workload (default, --config c4, the surrogate study's field): a seeded
+synthetic 384^3 float32 volume of 64 tubes (radius 1-3 voxels, 8-segment
+piecewise-linear centrelines) plus N(0, 0.05) noise -> 3x3 structure tensor
+(gradient, outer product, separable Gaussian sigma 1.5, 9 taps, same-size
+output) -> TK stick + plate voting at sigma 4 (w = 25, samples = 20; the
+plate is the exact orientation integral) -> per-voxel 3x3 eigendecomposition
+of the voted field.  --config c2 is the same recipe at 256^3.  One "step" is
+that whole pass over the volume; the metric is voxels per second.
 
   value     device-resident: input already in HBM, the pipeline call
             (tvgb_pipeline3) on device arrays, CUDA events on its stream,
@@ -213,7 +214,7 @@ def make_volume(cfg, dev=None):
 
 
 def metric_for(cfg):
-    if cfg["name"] == "C2":
+    if cfg["name"] in ("C2", "C4"):
         return METRIC
     return (f"3D tensor-vote voxels/s ({cfg['name']}: sigma={cfg['sigma']:g}, "
             f"stick+plate{'+ball' if cfg['ball'] else ''}, plain path)")
@@ -907,10 +908,11 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-surrogate", action="store_true", help="skip the surrogate-vs-plain study")
     ap.add_argument("--sur-block", type=int, default=64, help="edge of the surrogate study's interior block")
-    ap.add_argument("--sur-steps", type=int, default=40000, help="Adam steps of the surrogate's training")
-    ap.add_argument("--config", choices=["c2", "c4", "c5", "c3", "c1"], default="c2",
-                    help="c2: 3D pipeline, 256^3 (the headline); c4: the same at 384^3; c5: 512^3 tubes + sheets, "
-                         "sigma 6, stick + plate + ball (capacity); c3: batched 3x3 eigen; c1: 2D pipeline")
+    ap.add_argument("--sur-steps", type=int, default=100000, help="Adam steps of the surrogate's training")
+    ap.add_argument("--config", choices=["c2", "c4", "c5", "c3", "c1"], default="c4",
+                    help="c4: 3D pipeline at 384^3, sigma 4, the surrogate study's field (the headline); c2: the same "
+                         "at 256^3; c5: 512^3 tubes + sheets, sigma 6, stick + plate + ball (capacity); c3: batched "
+                         "3x3 eigen; c1: 2D pipeline")
     ap.add_argument("--split", choices=["replicas", "slabs"], default="replicas",
                     help="N > 1: independent replicas (weak scaling) or z-slabs of one volume (strong scaling)")
     ap.add_argument("--size", type=int, default=0, help="c2/c4/c5: volume edge (default 256/384/512); c3: log2 of "

@@ -89,10 +89,27 @@ static int device_pool(cudaMemPool_t& pool) {
     return TVGB_OK;
 }
 
+#ifndef TVGB_POOL_KIND
+#define TVGB_POOL_KIND 1
+#endif
 static int pool_alloc(void** ptr, size_t bytes, cudaStream_t s) {
+#if TVGB_POOL_KIND == 0
+    TVGB_CUDA(cudaMallocAsync(ptr, bytes, s));
+#elif TVGB_POOL_KIND == 2
+    static bool once = false;
+    if (!once) {
+        cudaMemPool_t dp;
+        cudaDeviceGetDefaultMemPool(&dp, 0);
+        unsigned long long keep = ~0ull;
+        cudaMemPoolSetAttribute(dp, cudaMemPoolAttrReleaseThreshold, &keep);
+        once = true;
+    }
+    TVGB_CUDA(cudaMallocAsync(ptr, bytes, s));
+#else
     cudaMemPool_t pool;
     TVGB_TRY(device_pool(pool));
     TVGB_CUDA(cudaMallocFromPoolAsync(ptr, bytes, pool, s));
+#endif
     return TVGB_OK;
 }
 
@@ -109,7 +126,9 @@ int DevArray::in(const void* p, size_t nbytes, cudaStream_t s) {
     TVGB_TRY(pool_alloc(&dev, nbytes, s));
     owned = true;
     scratch_track((long long)nbytes);
+    KernelTimer kt_("copy_h2d", s);   // the profile times staging copies beside the kernels
     TVGB_CUDA(cudaMemcpyAsync(dev, p, nbytes, cudaMemcpyHostToDevice, s));
+    kt_.stop();
     return TVGB_OK;
 }
 
@@ -131,8 +150,11 @@ int DevArray::out(void* p, size_t nbytes, cudaStream_t s, bool zero) {
 }
 
 int DevArray::finish() {
-    if (output && owned && dev && user)
+    if (output && owned && dev && user) {
+        KernelTimer kt_("copy_d2h", stream);
         TVGB_CUDA(cudaMemcpyAsync(user, dev, bytes, cudaMemcpyDeviceToHost, stream));
+        kt_.stop();
+    }
     return TVGB_OK;
 }
 

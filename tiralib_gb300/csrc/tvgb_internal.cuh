@@ -14,8 +14,16 @@ int structure_tensor3_device(const float* vol, unsigned s0, unsigned s1, unsigne
 void structure_tensor3_dims(unsigned s0, unsigned s1, unsigned s2, float sigma, int mode, unsigned* dims);
 
 // vote3.cu: voting on device arrays (in / out in the given layouts)
+// Called by vote3_device after the launch that votes receiver planes [z0, z1)
+// (in order, every plane once) when slab > 0.
+struct SlabHook {
+    int (*fn)(void* ctx, unsigned z0, unsigned z1);
+    void* ctx;
+    unsigned slab;   // receiver planes per launch; 0: one launch, no calls
+};
 int vote3_device(const float* in, int in_layout, unsigned s0, unsigned s1, unsigned s2, const tvgb_vote3_params& p,
-                 float* out, int out_layout, float* evals3, float* evecs, int evec_format, cudaStream_t s);
+                 float* out, int out_layout, float* evals3, float* evecs, int evec_format, cudaStream_t s,
+                 const SlabHook* hook = nullptr);
 
 // reconstruct.cu: SIMF of two (n, 4) fields into acc[0..2] = (<A,B>, <B,B>, sum of norms)
 int simf2_device(const float4* A, const float4* B, size_t n, double* acc3, cudaStream_t s);

@@ -139,6 +139,7 @@ struct FastArgs {
     float* evecs;
     int evec_fmt;
     int precise_eig;
+    int zr0, zr1;               // receivers voted: planes [zr0, zr1) (launch_fast: [0, s0) if empty)
 };
 
 __device__ __forceinline__ void kahan_add(float& sum, float& comp, float x) {
@@ -372,7 +373,7 @@ __global__ void __launch_bounds__(VX * VY, TVGB_FAST_MINB) k_vote3_fast(FastArgs
         tbl[2 * L2 + 1] = eb;
     }
 
-    const int x0 = blockIdx.x * VX, y0 = blockIdx.y * VY, z0 = blockIdx.z * R;
+    const int x0 = blockIdx.x * VX, y0 = blockIdx.y * VY, z0 = a.zr0 + int(blockIdx.z) * R;
     const int s0 = a.s0, s1 = a.s1, s2 = a.s2;
     const size_t plane = size_t(s1) * s2;
 
@@ -434,7 +435,7 @@ __global__ void __launch_bounds__(VX * VY, TVGB_FAST_MINB) k_vote3_fast(FastArgs
 #pragma unroll
     for (int j = 0; j < R; ++j) {
         const int z = z0 + j;
-        if (z >= s0) break;
+        if (z >= a.zr1) break;
         float m6[6];
 #pragma unroll
         for (int k = 0; k < 6; ++k) m6[k] = tot[j][k];
@@ -642,7 +643,7 @@ __global__ void __launch_bounds__(VX * VY, TVGB_FAST_MINB) k_vote3_pk(FastArgs a
         tbl[2 * L2] = ea;
         tbl[2 * L2 + 1] = eb;
     }
-    const int x0 = blockIdx.x * VX, y0 = blockIdx.y * VY, z0 = blockIdx.z * R;
+    const int x0 = blockIdx.x * VX, y0 = blockIdx.y * VY, z0 = a.zr0 + int(blockIdx.z) * R;
     const int s0 = a.s0, s1 = a.s1, s2 = a.s2;
     const size_t plane = size_t(s1) * s2;
     float tot[R][6], cmp[R][6];
@@ -740,7 +741,7 @@ __global__ void __launch_bounds__(VX * VY, TVGB_FAST_MINB) k_vote3_pk(FastArgs a
 #pragma unroll
     for (int j = 0; j < R; ++j) {
         const int z = z0 + j;
-        if (z >= s0) break;
+        if (z >= a.zr1) break;
         float m6[6];
 #pragma unroll
         for (int k = 0; k < 6; ++k) m6[k] = tot[j][k];
@@ -957,7 +958,7 @@ static int launch_fast_t(const FastArgs& a, cudaStream_t st) {
     const size_t smem = size_t(2 * nt) * 16 + (S ? size_t(SR) * SW * 16 : 0) + (P ? size_t(SR) * SW * 16 : 0) +
                         (B ? size_t(SR) * SW * 4 : 0);
     TVGB_CUDA(cudaFuncSetAttribute(k_vote3_fast<R, S, P, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-    dim3 grid(ceil_div(a.s2, VX), ceil_div(a.s1, VY), ceil_div(a.s0, R));
+    dim3 grid(ceil_div(a.s2, VX), ceil_div(a.s1, VY), ceil_div(size_t(a.zr1 - a.zr0), R));
     {
         KernelTimer kt_("k_vote3_fast", st);
         k_vote3_fast<R, S, P, B><<<grid, dim3(VX, VY), smem, st>>>(a);
@@ -978,7 +979,7 @@ static size_t fast_smem(int hw, int rows, bool S, bool P, bool B) {
 template <bool S, bool P, bool B>
 static int launch_pk_t(const FastArgs& a, size_t smem, cudaStream_t st) {
     TVGB_CUDA(cudaFuncSetAttribute(k_vote3_pk<S, P, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-    dim3 grid(ceil_div(a.s2, VX), ceil_div(a.s1, VY), ceil_div(a.s0, 4));
+    dim3 grid(ceil_div(a.s2, VX), ceil_div(a.s1, VY), ceil_div(size_t(a.zr1 - a.zr0), 4));
     {
         KernelTimer kt_("k_vote3_fast", st);
         k_vote3_pk<S, P, B><<<grid, dim3(VX, VY), smem, st>>>(a);
@@ -994,6 +995,8 @@ static size_t pk_smem(int hw, int rows, bool S, bool P, bool B) {
 }
 
 static int launch_fast(FastArgs a, bool S, bool P, bool B, cudaStream_t st) {
+    if (a.zr1 <= a.zr0) { a.zr0 = 0; a.zr1 = a.s0; }   // every receiver plane
+    if (a.zr1 <= a.zr0) return TVGB_OK;
     // rows per stage: the largest count that keeps TVGB_FAST_MINB CTAs per SM
     const int w = 2 * a.hw + 1;
     const size_t budget = (TVGB_FAST_MINB >= 3 ? 72 : 100) * 1024;
@@ -1059,7 +1062,8 @@ static int launch_prep(const float* in, int layout, size_t n, PrepOut o, float s
 }
 
 int vote3_device(const float* in, int in_layout, unsigned s0, unsigned s1, unsigned s2, const tvgb_vote3_params& p,
-                 float* out, int out_layout, float* evals3, float* evecs, int evec_format, cudaStream_t st) {
+                 float* out, int out_layout, float* evals3, float* evecs, int evec_format, cudaStream_t st,
+                 const SlabHook* hook) {
     const size_t n = size_t(s0) * s1 * s2;
     if (n == 0) return TVGB_OK;
     const unsigned w = p.w ? p.w : auto_window(p.sigma1, p.sigma2);
@@ -1094,7 +1098,17 @@ int vote3_device(const float* in, int in_layout, unsigned s0, unsigned s1, unsig
         if (out) TVGB_CUDA(cudaMemsetAsync(out, 0, n * (out_layout == TVGB_LAYOUT_MAT3 ? 36 : 24), st));
         if (!evals3 && !evecs) return TVGB_OK;
     }
-    if (fast) return launch_fast(fa, S, P, B, st);
+    if (fast) {
+        if (!hook || hook->slab == 0) return launch_fast(fa, S, P, B, st);
+        // receivers in z-slabs of hook->slab planes; the hook follows each slab's launch
+        for (unsigned z = 0; z < s0; z += hook->slab) {
+            fa.zr0 = int(z);
+            fa.zr1 = int(std::min(s0, z + hook->slab));
+            TVGB_TRY(launch_fast(fa, S, P, B, st));
+            TVGB_TRY(hook->fn(hook->ctx, unsigned(fa.zr0), unsigned(fa.zr1)));
+        }
+        return TVGB_OK;
+    }
 
     GenArgs g{};
     g.A = po.A; g.B = po.B; g.C = po.C; g.L = po.L; g.E1 = po.E1;
@@ -1122,6 +1136,7 @@ int vote3_device(const float* in, int in_layout, unsigned s0, unsigned s1, unsig
         kt_.stop();
     }
     TVGB_LAUNCHED();
+    if (hook && hook->slab) TVGB_TRY(hook->fn(hook->ctx, 0u, s0));   // one slab: the whole volume
     return TVGB_OK;
 }
 
