@@ -163,6 +163,24 @@ __device__ __forceinline__ void kahan_add(float& sum, float& comp, float x) {
 #endif
 constexpr int kDUnroll = TVGB_DUNROLL;
 
+// Block coordinates from the launch order: CTAs run roughly in linear-index
+// order (x fastest), and the plain mapping keeps z-neighbours, which share
+// most of their voter planes, a whole xy-layer apart.  In groups of ZG
+// z-blocks the order is x, then z within the group, then y, so the CTAs
+// resident at one time share their halos in L2.
+constexpr int ZG = 8;
+__device__ __forceinline__ void swizzled_block(int& bx, int& by, int& bz) {
+    const int gx = gridDim.x, gy = gridDim.y, gz = gridDim.z;
+    const int L = blockIdx.x + gx * (blockIdx.y + gy * blockIdx.z);
+    const int per = ZG * gx * gy;
+    const int g = L / per, rem = L - g * per;
+    const int gsz = min(ZG, gz - g * ZG);
+    bx = rem % gx;
+    const int t = rem / gx;
+    bz = g * ZG + t % gsz;
+    by = t / gsz;
+}
+
 // one (receiver, voter) pair: stick + closed-form plate (+ ball) into P[0..6]
 template <bool STICK, bool PLATE, bool BALL>
 __device__ __forceinline__ void vote_pair(const float4& A, const float4& B, float lb, float ub, float vb, float oxf,
@@ -373,7 +391,9 @@ __global__ void __launch_bounds__(VX * VY, TVGB_FAST_MINB) k_vote3_fast(FastArgs
         tbl[2 * L2 + 1] = eb;
     }
 
-    const int x0 = blockIdx.x * VX, y0 = blockIdx.y * VY, z0 = a.zr0 + int(blockIdx.z) * R;
+    int bx, by, bz;
+    swizzled_block(bx, by, bz);
+    const int x0 = bx * VX, y0 = by * VY, z0 = a.zr0 + bz * R;
     const int s0 = a.s0, s1 = a.s1, s2 = a.s2;
     const size_t plane = size_t(s1) * s2;
 
@@ -643,7 +663,9 @@ __global__ void __launch_bounds__(VX * VY, TVGB_FAST_MINB) k_vote3_pk(FastArgs a
         tbl[2 * L2] = ea;
         tbl[2 * L2 + 1] = eb;
     }
-    const int x0 = blockIdx.x * VX, y0 = blockIdx.y * VY, z0 = a.zr0 + int(blockIdx.z) * R;
+    int bx, by, bz;
+    swizzled_block(bx, by, bz);
+    const int x0 = bx * VX, y0 = by * VY, z0 = a.zr0 + bz * R;
     const int s0 = a.s0, s1 = a.s1, s2 = a.s2;
     const size_t plane = size_t(s1) * s2;
     float tot[R][6], cmp[R][6];
