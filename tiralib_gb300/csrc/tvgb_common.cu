@@ -89,27 +89,10 @@ static int device_pool(cudaMemPool_t& pool) {
     return TVGB_OK;
 }
 
-#ifndef TVGB_POOL_KIND
-#define TVGB_POOL_KIND 1
-#endif
 static int pool_alloc(void** ptr, size_t bytes, cudaStream_t s) {
-#if TVGB_POOL_KIND == 0
-    TVGB_CUDA(cudaMallocAsync(ptr, bytes, s));
-#elif TVGB_POOL_KIND == 2
-    static bool once = false;
-    if (!once) {
-        cudaMemPool_t dp;
-        cudaDeviceGetDefaultMemPool(&dp, 0);
-        unsigned long long keep = ~0ull;
-        cudaMemPoolSetAttribute(dp, cudaMemPoolAttrReleaseThreshold, &keep);
-        once = true;
-    }
-    TVGB_CUDA(cudaMallocAsync(ptr, bytes, s));
-#else
     cudaMemPool_t pool;
     TVGB_TRY(device_pool(pool));
     TVGB_CUDA(cudaMallocFromPoolAsync(ptr, bytes, pool, s));
-#endif
     return TVGB_OK;
 }
 
