@@ -203,3 +203,22 @@ def test_pipeline3_host_outputs_in_slabs_equal_device_outputs(out_layout, evecs)
     np.testing.assert_array_equal(o_h, o_d.cpu().numpy())
     np.testing.assert_array_equal(ev_h, ev_d.cpu().numpy())
     np.testing.assert_array_equal(vec_h, vec_d.cpu().numpy())
+
+
+def test_vote3_host_outputs_in_slabs_equal_device_outputs():
+    """tvgb_vote3 (behind tira::cuda::tensorvote3's drop-in) with host
+    arrays of a large field votes in z-slabs with the copies overlapped; the
+    results equal those written to device arrays bit for bit."""
+    import torch
+    import tiralib_gb300 as tv
+    rng = np.random.default_rng(9)
+    shape = (164, 160, 168)
+    A = rng.normal(size=(4096, 3, 3)).astype(np.float32)
+    T = (A @ np.swapaxes(A, -1, -2))[rng.integers(0, 4096, size=int(np.prod(shape)))].reshape(shape + (3, 3))
+    T = np.ascontiguousarray(T, np.float32)
+    kw = dict(w=9, samples=20, layout="mat3", out_layout="mat3", evals=True, evecs="spherical")
+    o_h, ev_h, vec_h = tv.vote3(T, 2.0, 0.0, **kw)
+    o_d, ev_d, vec_d = tv.vote3(torch.from_numpy(T).cuda(), 2.0, 0.0, **kw)
+    np.testing.assert_array_equal(o_h, o_d.cpu().numpy())
+    np.testing.assert_array_equal(ev_h, ev_d.cpu().numpy())
+    np.testing.assert_array_equal(vec_h, vec_d.cpu().numpy())

@@ -680,51 +680,6 @@ int tvgb_gaussian_convolve2(const float* src, unsigned in_sx, unsigned in_sy, fl
     return sync_if(din.owned || dout.owned, st);
 }
 
-namespace tvgb {
-// Host outputs of the 3D pipeline: the vote runs in z-slabs of receivers and
-// each slab's results go to the host on a second stream while the next slab
-// votes.  A device->host copy into host memory that has not been touched by
-// the GPU for a while runs well below the link's rate, so leaving the whole
-// result for the end cost a fifth of the 384^3 pipeline's time.
-struct SlabCopy {
-    struct Out {
-        float* host;
-        const float* dev;
-        size_t per;      // floats per voxel
-        bool planes;     // component planes (per planes of n floats) rather than interleaved
-    };
-    cudaStream_t compute = nullptr, copy = nullptr;
-    std::vector<cudaEvent_t> events;
-    Out outs[3];
-    int nout = 0;
-    size_t plane = 0, n = 0;   // voxels per z-plane, voxels in all
-};
-
-static int slab_copy(void* ctx, unsigned z0, unsigned z1) {
-    SlabCopy& c = *static_cast<SlabCopy*>(ctx);
-    cudaEvent_t e = nullptr;
-    TVGB_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-    c.events.push_back(e);
-    TVGB_CUDA(cudaEventRecord(e, c.compute));
-    TVGB_CUDA(cudaStreamWaitEvent(c.copy, e, 0));
-    const size_t v0 = size_t(z0) * c.plane, nv = size_t(z1 - z0) * c.plane;
-    for (int i = 0; i < c.nout; ++i) {
-        const SlabCopy::Out& o = c.outs[i];
-        KernelTimer kt_("copy_d2h", c.copy);
-        if (o.planes) {
-            for (size_t k = 0; k < o.per; ++k)
-                TVGB_CUDA(cudaMemcpyAsync(o.host + k * c.n + v0, o.dev + k * c.n + v0, nv * sizeof(float),
-                                          cudaMemcpyDeviceToHost, c.copy));
-        } else {
-            TVGB_CUDA(cudaMemcpyAsync(o.host + v0 * o.per, o.dev + v0 * o.per, nv * o.per * sizeof(float),
-                                      cudaMemcpyDeviceToHost, c.copy));
-        }
-        kt_.stop();
-    }
-    return TVGB_OK;
-}
-}  // namespace tvgb
-
 int tvgb_pipeline3(const float* volume, unsigned s0, unsigned s1, unsigned s2, float sigma_st, int st_mode,
                    const tvgb_vote3_params* p, float* out, int out_layout, float* evals3, float* evecs, int evec_format,
                    unsigned* out_dims, void* stream) {
@@ -762,35 +717,14 @@ int tvgb_pipeline3(const float* volume, unsigned s0, unsigned s1, unsigned s2, f
         TVGB_TRY(dvec.finish());
         return sync_if(din.owned || host_out, st);
     }
-    // host outputs of a large volume: about 8 slabs of receiver planes, copies overlapped with the vote
-    SlabCopy c;
-    c.compute = st;
-    c.plane = size_t(d[1]) * d[2];
-    c.n = no;
-    if (dout.owned) c.outs[c.nout++] = {out, dout.get<float>(), nout, out_layout == TVGB_LAYOUT_SYM6_PLANES};
-    if (dev_.owned) c.outs[c.nout++] = {evals3, dev_.get<float>(), 3, false};
-    if (dvec.owned) c.outs[c.nout++] = {evecs, dvec.get<float>(), nv, false};
-    TVGB_CUDA(cudaStreamCreateWithFlags(&c.copy, cudaStreamNonBlocking));
-    SlabHook hook{slab_copy, &c, std::max(4u, ((d[0] + 7) / 8 + 3) / 4 * 4)};
-    int rc = vote3_device(tensor.get<float>(), TVGB_LAYOUT_SYM6_PLANES, d[0], d[1], d[2], *p, dout.get<float>(),
-                          out_layout, dev_.get<float>(), dvec.get<float>(), nv ? evec_format : 0, st, &hook);
-    // join the copy stream before the device temporaries are released on st
-    cudaEvent_t done = nullptr;
-    if (cudaEventCreateWithFlags(&done, cudaEventDisableTiming) == cudaSuccess &&
-        cudaEventRecord(done, c.copy) == cudaSuccess) {
-        cudaStreamWaitEvent(st, done, 0);
-    } else {
-        cudaStreamSynchronize(c.copy);
-    }
-    const cudaError_t se = cudaStreamSynchronize(st);
-    if (done) cudaEventDestroy(done);
-    for (cudaEvent_t e : c.events) cudaEventDestroy(e);
-    cudaStreamDestroy(c.copy);
-    if (rc != TVGB_OK) return rc;
-    if (se != cudaSuccess) {
-        set_error("tvgb_pipeline3: %s", cudaGetErrorString(se));
-        return TVGB_ERR_CUDA;
-    }
+    // host outputs of a large volume: z-slabs, copies overlapped with the vote
+    HostOut outs[3];
+    int no_ = 0;
+    if (dout.owned) outs[no_++] = {out, dout.get<float>(), nout, out_layout == TVGB_LAYOUT_SYM6_PLANES};
+    if (dev_.owned) outs[no_++] = {evals3, dev_.get<float>(), 3, false};
+    if (dvec.owned) outs[no_++] = {evecs, dvec.get<float>(), nv, false};
+    TVGB_TRY(vote3_to_host(tensor.get<float>(), TVGB_LAYOUT_SYM6_PLANES, d[0], d[1], d[2], *p, dout.get<float>(),
+                           out_layout, dev_.get<float>(), dvec.get<float>(), nv ? evec_format : 0, outs, no_, st));
     return TVGB_OK;
 }
 

@@ -24,6 +24,19 @@ struct SlabHook {
 int vote3_device(const float* in, int in_layout, unsigned s0, unsigned s1, unsigned s2, const tvgb_vote3_params& p,
                  float* out, int out_layout, float* evals3, float* evecs, int evec_format, cudaStream_t s,
                  const SlabHook* hook = nullptr);
+// A host output of a vote and the device temporary it is computed in.
+struct HostOut {
+    float* host;
+    const float* dev;
+    size_t per;      // floats per voxel
+    bool planes;     // per component planes of n floats rather than interleaved
+};
+// vote3_device in z-slabs, each slab's part of every HostOut copied to the
+// host on a second stream while the next slab votes; returns after all of
+// it has completed (st synchronised).
+int vote3_to_host(const float* in, int in_layout, unsigned s0, unsigned s1, unsigned s2, const tvgb_vote3_params& p,
+                  float* out, int out_layout, float* evals3, float* evecs, int evec_format, const HostOut* outs,
+                  int nouts, cudaStream_t s);
 
 // reconstruct.cu: SIMF of two (n, 4) fields into acc[0..2] = (<A,B>, <B,B>, sum of norms)
 int simf2_device(const float4* A, const float4* B, size_t n, double* acc3, cudaStream_t s);

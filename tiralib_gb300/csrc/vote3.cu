@@ -38,6 +38,8 @@
 // sphere, scaled by lambda0) is (c1/3 + ct [o != 0] / 15) I + (2 ct g / 15) o o^T.
 #include "tvgb_internal.cuh"
 #include "eig_device.cuh"
+#include <algorithm>
+#include <vector>
 
 namespace tvgb {
 
@@ -1162,6 +1164,76 @@ int vote3_device(const float* in, int in_layout, unsigned s0, unsigned s1, unsig
     return TVGB_OK;
 }
 
+// Host outputs of a large vote: the receivers are voted in z-slabs and each
+// slab's results go to the host on a second stream while the next slab
+// votes.  A device->host copy into host memory the GPU has not touched for a
+// while runs well below the link's rate, so leaving the whole result for the
+// end cost a fifth of the 384^3 pipeline's time.
+struct SlabCopy {
+    cudaStream_t compute = nullptr, copy = nullptr;
+    std::vector<cudaEvent_t> events;
+    const HostOut* outs = nullptr;
+    int nout = 0;
+    size_t plane = 0, n = 0;   // voxels per z-plane, voxels in all
+};
+
+static int slab_copy(void* ctx, unsigned z0, unsigned z1) {
+    SlabCopy& c = *static_cast<SlabCopy*>(ctx);
+    cudaEvent_t e = nullptr;
+    TVGB_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    c.events.push_back(e);
+    TVGB_CUDA(cudaEventRecord(e, c.compute));
+    TVGB_CUDA(cudaStreamWaitEvent(c.copy, e, 0));
+    const size_t v0 = size_t(z0) * c.plane, nv = size_t(z1 - z0) * c.plane;
+    for (int i = 0; i < c.nout; ++i) {
+        const HostOut& o = c.outs[i];
+        KernelTimer kt_("copy_d2h", c.copy);
+        if (o.planes) {
+            for (size_t k = 0; k < o.per; ++k)
+                TVGB_CUDA(cudaMemcpyAsync(o.host + k * c.n + v0, o.dev + k * c.n + v0, nv * sizeof(float),
+                                          cudaMemcpyDeviceToHost, c.copy));
+        } else {
+            TVGB_CUDA(cudaMemcpyAsync(o.host + v0 * o.per, o.dev + v0 * o.per, nv * o.per * sizeof(float),
+                                      cudaMemcpyDeviceToHost, c.copy));
+        }
+        kt_.stop();
+    }
+    return TVGB_OK;
+}
+
+int vote3_to_host(const float* in, int in_layout, unsigned s0, unsigned s1, unsigned s2, const tvgb_vote3_params& p,
+                  float* out, int out_layout, float* evals3, float* evecs, int evec_format, const HostOut* outs,
+                  int nouts, cudaStream_t st) {
+    SlabCopy c;
+    c.compute = st;
+    c.plane = size_t(s1) * s2;
+    c.n = size_t(s0) * c.plane;
+    c.outs = outs;
+    c.nout = nouts;
+    TVGB_CUDA(cudaStreamCreateWithFlags(&c.copy, cudaStreamNonBlocking));
+    // about 8 slabs, each a multiple of the kernels' 4-plane receiver groups
+    SlabHook hook{slab_copy, &c, std::max(4u, ((s0 + 7) / 8 + 3) / 4 * 4)};
+    const int rc = vote3_device(in, in_layout, s0, s1, s2, p, out, out_layout, evals3, evecs, evec_format, st, &hook);
+    // join the copy stream before the caller releases the device temporaries on st
+    cudaEvent_t done = nullptr;
+    if (cudaEventCreateWithFlags(&done, cudaEventDisableTiming) == cudaSuccess &&
+        cudaEventRecord(done, c.copy) == cudaSuccess) {
+        cudaStreamWaitEvent(st, done, 0);
+    } else {
+        cudaStreamSynchronize(c.copy);
+    }
+    const cudaError_t se = cudaStreamSynchronize(st);
+    if (done) cudaEventDestroy(done);
+    for (cudaEvent_t e : c.events) cudaEventDestroy(e);
+    cudaStreamDestroy(c.copy);
+    if (rc != TVGB_OK) return rc;
+    if (se != cudaSuccess) {
+        set_error("vote with host outputs: %s", cudaGetErrorString(se));
+        return TVGB_ERR_CUDA;
+    }
+    return TVGB_OK;
+}
+
 }  // namespace tvgb
 
 using namespace tvgb;
@@ -1199,12 +1271,22 @@ int tvgb_vote3(const float* in, int in_layout, unsigned s0, unsigned s1, unsigne
     TVGB_TRY(dout.out(out, n * nout * 4, st));
     TVGB_TRY(dev_.out(evals3, n * 12, st));
     TVGB_TRY(dvec.out(nv ? evecs : nullptr, n * nv * 4, st));
+    const bool host_out = dout.owned || dev_.owned || dvec.owned;
+    if (host_out && n >= (size_t(1) << 22)) {   // large volume, host outputs: copies overlapped with the vote
+        HostOut outs[3];
+        int no_ = 0;
+        if (dout.owned) outs[no_++] = {out, dout.get<float>(), nout, out_layout == TVGB_LAYOUT_SYM6_PLANES};
+        if (dev_.owned) outs[no_++] = {evals3, dev_.get<float>(), 3, false};
+        if (dvec.owned) outs[no_++] = {evecs, dvec.get<float>(), nv, false};
+        return vote3_to_host(din.get<float>(), in_layout, s0, s1, s2, *p, dout.get<float>(), out_layout,
+                             dev_.get<float>(), dvec.get<float>(), nv ? evec_format : 0, outs, no_, st);
+    }
     TVGB_TRY(vote3_device(din.get<float>(), in_layout, s0, s1, s2, *p, dout.get<float>(), out_layout,
                           dev_.get<float>(), dvec.get<float>(), nv ? evec_format : 0, st));
     TVGB_TRY(dout.finish());
     TVGB_TRY(dev_.finish());
     TVGB_TRY(dvec.finish());
-    return sync_if(din.owned || dout.owned || dev_.owned || dvec.owned, st);
+    return sync_if(din.owned || host_out, st);
 }
 
 int tvgb_tensorvote3(const float* input_field, float* output_field, unsigned s0, unsigned s1, unsigned s2, float sigma,
