@@ -242,8 +242,8 @@ int tvgb_simf2(const float* A, const float* B, size_t n, double* simf, void* str
 int tvgb_tensorvote_sweep(const float* t_in, const float* G, unsigned shape0, unsigned shape1, const double* params,
                           int K, unsigned samples, int plate, double* simf, float* t_out, void* stream);
 
-/* ---- Learned plate / ball vote (no reference counterpart: the north-star
- * surrogate of the reference's plate3_numerical_device, tensorvote.h:2457).
+/* ---- Learned plate / ball vote (no reference counterpart: a learned
+ * stand-in for the reference's plate3_numerical_device, tensorvote.h:2457).
  * The network is an MLP 7 -> 64 -> 64 -> 64 -> 6 (GELU; BF16 weights and
  * activations on the tensor cores, FP32 accumulation) from
  * (offset direction o / |o|, plate normal n, flag: 1 plate / 0 ball) to the
