@@ -481,7 +481,7 @@ def surrogate_study(vol_d, cfg, args, dev):
     t0 = time.perf_counter()
     X, T = S.samples(1 << 24, seed=4, device=dev)
     p = S.init_params(0)
-    hist = S.train(p, X, T, batch=8192, steps=args.sur_steps, lr=3e-3)
+    hist = S.train(p, X, T, batch=8192, steps=args.sur_steps, lr=args.sur_lr)
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
     del X, T
@@ -520,7 +520,7 @@ def surrogate_study(vol_d, cfg, args, dev):
                   f"{cfg['sigma']:g}, w {cfg['w']}; stick exact, plate by the rule named; ball off",
         "network": f"7-64-64-64-6 GELU, BF16 weights and activations, FP32 accumulation, tcgen05.mma with the "
                    f"activations in tensor memory; trained here on 2^24 plain-integral samples, {args.sur_steps} "
-                   f"Adam steps of 8192",
+                   f"Adam steps of 8192 (lr {args.sur_lr:g}, cosine decay)",
         "train_s": t_train, "final_loss": float(np.mean(hist[-100:])), "heldout_rel_err": heldout,
         "kernel_ms": kms, "voxels_per_s": vps,
         "surrogate_vs_plain64": vps["surrogate_unjudged"] / vps["plain64"],
@@ -910,6 +910,7 @@ def main():
     ap.add_argument("--no-surrogate", action="store_true", help="skip the surrogate-vs-plain study")
     ap.add_argument("--sur-block", type=int, default=64, help="edge of the surrogate study's interior block")
     ap.add_argument("--sur-steps", type=int, default=100000, help="Adam steps of the surrogate's training")
+    ap.add_argument("--sur-lr", type=float, default=6e-3, help="peak learning rate of the surrogate's training")
     ap.add_argument("--config", choices=["c2", "c4", "c5", "c3", "c1"], default="c4",
                     help="c4: 3D pipeline at 384^3, sigma 4, the surrogate study's field (the headline); c2: the same "
                          "at 256^3; c5: 512^3 tubes + sheets, sigma 6, stick + plate + ball (capacity); c3: batched "
