@@ -161,7 +161,7 @@ def gpu_index_for(local_rank):
     return local_rank
 
 
-def cpu_reference_sample(vol, cfg, block=16, seed=0, threads=None):
+def cpu_reference_sample(vol, cfg, block=16, seed=0, threads=None, detail=None):
     """The reference's CPU algorithm on one bounded sample: an interior
     block^3 receiver block with its window halo.  Structure tensor (oracle
     restatement of volume::gradient + gaussian_convolve3), cpu::tensorvote3's
@@ -191,8 +191,86 @@ def cpu_reference_sample(vol, cfg, block=16, seed=0, threads=None):
     out = O.tensorvote3_receivers(m9, rec, cfg["sigma"], 0.0, cfg["w"], 1, samples=cfg["samples"], threads=threads)
     voted = out.reshape(-1, 9)[rec]
     ev = O.evals3(voted)
-    O.evecs3cart(voted, ev)
-    return time.perf_counter() - t0, rec.size, threads
+    vec = O.evecs3cart(voted, ev)
+    dt = time.perf_counter() - t0
+    if detail is not None:
+        detail.update(block=(z0, y0, x0, block), field=m9, receivers=rec, voted=voted, evals=ev, evecs=vec)
+    return dt, rec.size, threads
+
+
+def accuracy_against_cpu(detail, cfg, out_d, ev_d, vec_d, threads, precise=None):
+    """The GPU pipeline's results at the CPU sample's receivers against (a)
+    the reference's algorithm on the CPU (oracle port, same input volume,
+    its own structure tensor) and (b) the FP64 oracle (FP64 eigenvectors of
+    the voters, FP64 vote) on that structure tensor.  Voted tensors: the six
+    entries eigen.h reads back; per receiver ||d|| / ||ref|| (Frobenius over
+    the six), and max|d| / max|ref| over the block.  Eigenvalues: per
+    receiver max|d| / max|ref|.  Eigenvectors: angle between matching
+    vectors (up to sign), largest and smallest."""
+    from oracle import oracle as O
+    z0, y0, x0, b = detail["block"]
+    sl = (slice(z0, z0 + b), slice(y0, y0 + b), slice(x0, x0 + b))
+    g6 = np.moveaxis(out_d[(slice(None),) + sl].cpu().numpy(), 0, -1).reshape(-1, 6).astype(np.float64)
+    gev = ev_d[sl].cpu().numpy().reshape(-1, 3).astype(np.float64)
+    gvec = vec_d[sl].cpu().numpy().reshape(-1, 3, 3).astype(np.float64)
+    idx6 = [0, 1, 2, 4, 5, 8]
+    c6 = detail["voted"].reshape(-1, 9)[:, idx6].astype(np.float64)
+    f64 = O.tensorvote3_f64(detail["field"], cfg["sigma"], 0.0, cfg["w"], 1, ball=cfg["ball"],
+                            receivers=detail["receivers"], threads=threads).reshape(-1, 6)[detail["receivers"]]
+    wgt = np.array([1, 2, 2, 1, 2, 1], np.float64)   # off-diagonal entries count twice in the Frobenius norm
+
+    def tensor_err(a, ref):
+        per = np.sqrt((wgt * (a - ref) ** 2).sum(1) / np.maximum((wgt * ref ** 2).sum(1), 1e-300))
+        return {"per_receiver_max": float(per.max()), "per_receiver_median": float(np.median(per)),
+                "max_abs_over_max": float(np.abs(a - ref).max() / np.abs(ref).max())}
+
+    cev = detail["evals"].astype(np.float64)
+    ev_rel = np.abs(gev - cev).max(1) / np.maximum(np.abs(cev).max(1), 1e-300)
+    cvec = detail["evecs"].reshape(-1, 3, 3).astype(np.float64)
+    cosang = np.clip(np.abs((gvec * cvec).sum(2)), 0.0, 1.0)          # rows e0, e1, e2
+    ang = np.arccos(cosang)
+    out = {"receivers": int(b ** 3), "block_origin_zyx": [int(z0), int(y0), int(x0)],
+           "voted_vs_reference_cpu": tensor_err(g6, c6),
+           "voted_vs_fp64": tensor_err(g6, f64),
+           "eigenvalues_vs_reference_cpu": {"max": float(ev_rel.max()), "median": float(np.median(ev_rel))},
+           "eigenvector_angle_rad_vs_reference_cpu": {"e2_max": float(ang[:, 2].max()),
+                                                      "e2_median": float(np.median(ang[:, 2])),
+                                                      "e0_max": float(ang[:, 0].max()),
+                                                      "e0_median": float(np.median(ang[:, 0]))}}
+    out["note_fp64"] = ("the reference's eigen.h thresholds are absolute (1e-6 on b^2+d^2+e^2): the noise voxels' "
+                        "structure tensors fall under them, so the reference's voter eigenvectors, which parity "
+                        "mode reproduces, are far from FP64's; precise mode (scaled, relative thresholds, FP64 "
+                        "refinement of near-degenerate pairs) is the one to judge against FP64")
+    if precise is not None:
+        p_out, p_ev, p_vec = precise
+        p6 = np.moveaxis(p_out[(slice(None),) + sl].cpu().numpy(), 0, -1).reshape(-1, 6).astype(np.float64)
+        pev = p_ev[sl].cpu().numpy().reshape(-1, 3).astype(np.float64)
+        pvec = p_vec[sl].cpu().numpy().reshape(-1, 3, 3).astype(np.float64)
+        fev, fvec = O.eig3_f64(f64)
+        prel = np.abs(pev - fev).max(1) / np.maximum(np.abs(fev).max(1), 1e-300)
+        pang = np.arccos(np.clip(np.abs((pvec * fvec).sum(2)), 0.0, 1.0))
+        # the eigensolver alone: FP64 Jacobi of the GPU's own voted tensors
+        sev, svec = O.eig3_f64(p6)
+        srel = np.abs(pev - sev).max(1) / np.maximum(np.abs(sev).max(1), 1e-300)
+        sang = np.arccos(np.clip(np.abs((pvec * svec).sum(2)), 0.0, 1.0))
+        out["precise_mode"] = {
+            "voted_vs_fp64": tensor_err(p6, f64),
+            "eigenvalues_vs_fp64": {"max": float(prel.max()), "median": float(np.median(prel))},
+            "eigenvector_angle_rad_vs_fp64": {"e2_max": float(pang[:, 2].max()),
+                                              "e2_median": float(np.median(pang[:, 2])),
+                                              "e0_max": float(pang[:, 0].max()),
+                                              "e0_median": float(np.median(pang[:, 0]))},
+            "eigensolver_alone": {"eigenvalues_max": float(srel.max()), "eigenvalues_median": float(np.median(srel)),
+                                  "angle_rad_e2_max": float(sang[:, 2].max()),
+                                  "angle_rad_e2_median": float(np.median(sang[:, 2])),
+                                  "angle_rad_e0_max": float(sang[:, 0].max()),
+                                  "angle_rad_e0_median": float(np.median(sang[:, 0]))},
+            "note": "the eigenvector angles against the FP64 vote follow the voted tensors' own FP32 error divided "
+                    "by their eigenvalue gaps; eigensolver_alone compares with FP64 Jacobi of the same tensors"}
+    if cfg["ball"]:
+        out["note_ball"] = ("the reference's CPU algorithm has no TK ball term: voted_vs_reference_cpu includes the "
+                            "GPU's ball vote; the FP64 comparisons include it on both sides")
+    return out
 
 
 def config3(args):
@@ -434,8 +512,19 @@ def run_ours(args, rank, world, local_rank):
         sur = surrogate_study(vol_d, cfg, args, dev)
 
     cpu = None
+    accuracy = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        t, nrec, th = cpu_reference_sample(vol_np, cfg, block=args.ref_block, seed=0)
+        detail = {}
+        t, nrec, th = cpu_reference_sample(vol_np, cfg, block=args.ref_block, seed=0, detail=detail)
+        if not strong:
+            # the same pipeline in precise mode (outside every timed region), for the FP64 comparison
+            p_out = torch.empty_like(out_d)
+            p_ev = torch.empty_like(ev_d)
+            p_vec = torch.empty_like(vec_d)
+            tv.pipeline3(vol_d, outputs=(p_out, p_ev, p_vec), parity=False, **kw)
+            torch.cuda.synchronize()
+            accuracy = accuracy_against_cpu(detail, cfg, out_d, ev_d, vec_d, th, precise=(p_out, p_ev, p_vec))
+            del p_out, p_ev, p_vec
         cpu = {"value": nrec / t, "unit": "voxels/s", "cores": th, "kind": "port",
                "sample": f"{args.ref_block}^3 interior receivers of the same volume (+ window halo), the reference's "
                          f"CPU algorithm (stick + {cfg['samples']}-sample plate"
@@ -451,7 +540,7 @@ def run_ours(args, rank, world, local_rank):
             "e2e": {"value": e2e_value, "unit": "voxels/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
             "kernels": {k: {"launches": v[0], "total_ms": v[1]} for k, v in prof.items()},
-            "memory": memory, "surrogate": sur,
+            "memory": memory, "surrogate": sur, "accuracy": accuracy,
         }
         print(json.dumps(line), flush=True)
     if dist:
