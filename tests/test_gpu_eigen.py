@@ -66,6 +66,35 @@ def test_eig3_fused_matches_oracle(tv, layout, fmt):
         assert np.abs(np.cos(vec) - np.cos(ref)).max() < 1e-3
 
 
+@pytest.mark.parametrize("precise", [False, True])
+@pytest.mark.parametrize("layout", ["mat3", "sym6", "planes"])
+def test_eig3_many_tiles_per_block(tv, layout, precise):
+    """2^20 + 37 tensors: every block of the grid-stride solver works through
+    several tiles, each staged while the previous one is solved (the AoS
+    layouts), ending with a ragged tile."""
+    rng = np.random.default_rng(11)
+    n = (1 << 20) + 37
+    A = rng.normal(size=(n, 3, 3)).astype(np.float32)
+    M = (A @ np.swapaxes(A, 1, 2)).astype(np.float32)
+    m9 = M.reshape(n, 9)
+    if layout == "mat3":
+        inp = m9
+    elif layout == "sym6":
+        inp = np.ascontiguousarray(m9[:, UNIQUE9])
+    else:
+        inp = np.ascontiguousarray(m9[:, UNIQUE9].T)
+    ev, vec, _ = tv.eig3(inp, layout=layout, evecs="cartesian", precise=precise)
+    ref_ev = O.evals3(m9)
+    assert evals_rel(ev, ref_ev) < 1e-4
+    ref = O.evecs3cart(m9, ref_ev)
+    lam = ref_ev.astype(np.float64)
+    scale = np.abs(lam).max(axis=1)
+    sep = np.minimum(lam[:, 1] - lam[:, 0], lam[:, 2] - lam[:, 1]) > 1e-2 * scale   # well separated
+    dots = np.abs(np.einsum("nij,nij->ni", vec[sep], ref[sep]))
+    assert sep.sum() > n // 2
+    assert (1.0 - dots).max() < 1e-4
+
+
 def test_eig3_empty_and_device(tv):
     import torch
     ev, vec, _ = tv.eig3(np.zeros((0, 9), np.float32))

@@ -327,16 +327,39 @@ __device__ __forceinline__ int eig3_precise_fp32(float a, float b, float c, floa
     return 0;
 }
 
+// Conversions between FP32 and FP64 on the integer pipe.  GB300's FP64 pipe
+// executes conversions at its own low rate, and in the FP64 phase below they
+// were as many as its arithmetic operations.
+// widen_f32: exact for normal floats; zero and subnormal inputs give a signed
+// zero; the input is finite.
+__device__ __forceinline__ double widen_f32(float x) {
+    const unsigned u = __float_as_uint(x), mag = u & 0x7fffffffu;
+    const bool nrm = mag >= 0x00800000u;
+    const unsigned hi = (u & 0x80000000u) | (nrm ? (mag >> 3) + (896u << 20) : 0u);   // exponent bias 1023 - 127
+    return __hiloint2double(int(hi), int(nrm ? u << 29 : 0u));
+}
+// narrow_trunc: the mantissa truncated to 24 bits (relative error < 2^-23);
+// magnitudes below the FP32 normal range give a signed zero; |x| < 2^128.
+__device__ __forceinline__ float narrow_trunc(double x) {
+    const unsigned hi = unsigned(__double2hiint(x)), lo = unsigned(__double2loint(x));
+    const unsigned mag = hi & 0x7fffffffu, sgn = hi & 0x80000000u;
+    if ((mag >> 20) <= 896u) return __uint_as_float(sgn);
+    return __uint_as_float(sgn | ((mag - (896u << 20)) << 3) | (lo >> 29));
+}
+
 // FP64 phase.  code 1: the pair is resolved on the plane normal to w.  The
 // plane basis is exact: U = e_k x w copies two components of w (k = the
 // smallest |w_k|), V = w x U is formed in FP64, so w, U, V are orthogonal to
-// FP64 rounding and |V|^2 = |w|^2 |U|^2.  The 2x2 matrix H = [U V]^T A [U V]
-// is formed in FP64; with the Gram scaling folded in (H' = diag(1, 1/|w|)
-// H diag(1, 1/|w|) / |U|^2, |w|^2 = 1 + O(eps32) so 1/|w| and 1/|w|^2 are
-// two-term series) its difference and off-diagonal, which cancel for a close
-// pair, are exact to FP64 rounding.  The Jacobi angle needs only FP32
-// relative accuracy from those two numbers, the pair's eigenvalues come from
-// the rotated FP64 diagonal, and the frame is completed in FP32.
+// FP64 rounding and |V|^2 = |w|^2 |U|^2.  The work is done in the frame
+// rotated cyclically to put axis k first, where U = (0, -w2, w1) and
+// V = (w1^2 + w2^2, -w0 w1, -w0 w2) (products of two floats, exact in FP64).
+// The 2x2 matrix H = [U V]^T A [U V] is formed in FP64; with the Gram scaling
+// folded in (H' = diag(1, 1/|w|) H diag(1, 1/|w|) / |U|^2, |w|^2 = 1 +
+// O(eps32) so 1/|w| and 1/|w|^2 are two-term series) its difference and
+// off-diagonal, which cancel for a close pair, are exact to FP64 rounding.
+// The Jacobi angle needs only FP32 relative accuracy from those two numbers,
+// the pair's eigenvalues come from the rotated FP64 diagonal, and the frame
+// is completed in FP32.  41 FP64 operations in all.
 // code 2: cyclic Jacobi on the whole matrix in FP64.
 __device__ __forceinline__ void eig3_precise_fp64(float a, float b, float c, float d, float e, float f, const float* w,
                                                   bool iso_high, int code, float* ev, float* v0, float* v1, float* v2) {
@@ -346,23 +369,32 @@ __device__ __forceinline__ void eig3_precise_fp64(float a, float b, float c, flo
     const float sc = ldexpf(1.0f, 1 - ex), unsc = ldexpf(1.0f, ex - 1);
     if (code == 1) {
         const float Af[6] = {a * sc, b * sc, d * sc, c * sc, e * sc, f * sc};   // xx xy xz yy yz zz
-        const double A[6] = {Af[0], Af[1], Af[2], Af[3], Af[4], Af[5]};
         const float aw0 = fabsf(w[0]), aw1 = fabsf(w[1]), aw2 = fabsf(w[2]);
         const int k = (aw0 <= aw1 && aw0 <= aw2) ? 0 : (aw1 <= aw2 ? 1 : 2);
-        float Uf[3];   // e_k x w, exact
-        if (k == 0) { Uf[0] = 0.0f; Uf[1] = -w[2]; Uf[2] = w[1]; }
-        else if (k == 1) { Uf[0] = w[2]; Uf[1] = 0.0f; Uf[2] = -w[0]; }
-        else { Uf[0] = -w[1]; Uf[1] = w[0]; Uf[2] = 0.0f; }
-        const double w0 = w[0], w1 = w[1], w2 = w[2], U0 = Uf[0], U1 = Uf[1], U2 = Uf[2];
-        const double V0 = w1 * U2 - w2 * U1, V1 = w2 * U0 - w0 * U2, V2 = w0 * U1 - w1 * U0;
-        const double nw = fma(w0, w0, fma(w1, w1, w2 * w2));
-        const double AU0 = fma(A[0], U0, fma(A[1], U1, A[2] * U2));
-        const double AU1 = fma(A[1], U0, fma(A[3], U1, A[4] * U2));
-        const double AU2 = fma(A[2], U0, fma(A[4], U1, A[5] * U2));
-        const double AV0 = fma(A[0], V0, fma(A[1], V1, A[2] * V2));
-        const double AV1 = fma(A[1], V0, fma(A[3], V1, A[4] * V2));
-        const double AV2 = fma(A[2], V0, fma(A[4], V1, A[5] * V2));
-        const double h00 = fma(U0, AU0, fma(U1, AU1, U2 * AU2));
+        // A and w in the frame (k, k + 1, k + 2 mod 3)
+        float p00, p01, p02, p11, p12, p22, s0, s1, s2;
+        if (k == 0) {
+            p00 = Af[0]; p11 = Af[3]; p22 = Af[5]; p01 = Af[1]; p02 = Af[2]; p12 = Af[4];
+            s0 = w[0]; s1 = w[1]; s2 = w[2];
+        } else if (k == 1) {
+            p00 = Af[3]; p11 = Af[5]; p22 = Af[0]; p01 = Af[4]; p02 = Af[1]; p12 = Af[2];
+            s0 = w[1]; s1 = w[2]; s2 = w[0];
+        } else {
+            p00 = Af[5]; p11 = Af[0]; p22 = Af[3]; p01 = Af[2]; p02 = Af[4]; p12 = Af[1];
+            s0 = w[2]; s1 = w[0]; s2 = w[1];
+        }
+        const double P00 = widen_f32(p00), P01 = widen_f32(p01), P02 = widen_f32(p02), P11 = widen_f32(p11),
+                     P12 = widen_f32(p12), P22 = widen_f32(p22);
+        const double W0 = widen_f32(s0), W1 = widen_f32(s1), W2 = widen_f32(s2);
+        const double V0 = fma(W1, W1, W2 * W2), V1 = -(W0 * W1), V2 = -(W0 * W2);
+        const double nw = fma(W0, W0, V0);
+        const double AU0 = fma(P02, W1, -(P01 * W2));                 // A U, U = (0, -W2, W1)
+        const double AU1 = fma(P12, W1, -(P11 * W2));
+        const double AU2 = fma(P22, W1, -(P12 * W2));
+        const double AV0 = fma(P00, V0, fma(P01, V1, P02 * V2));
+        const double AV1 = fma(P01, V0, fma(P11, V1, P12 * V2));
+        const double AV2 = fma(P02, V0, fma(P12, V1, P22 * V2));
+        const double h00 = fma(W1, AU2, -(W2 * AU1));
         const double h01 = fma(V0, AU0, fma(V1, AU1, V2 * AU2));
         const double h11 = fma(V0, AV0, fma(V1, AV1, V2 * AV2));
         const double dn = nw - 1.0;                                  // |dn| ~ 1e-7
@@ -370,25 +402,37 @@ __device__ __forceinline__ void eig3_precise_fp64(float a, float b, float c, flo
         const double isq = fma(0.375 * dn, dn, 1.0 - 0.5 * dn);      // 1 / |w|
         const double g11 = h11 * inw, g01 = h01 * isq;               // |U|^2 H'
         // Jacobi rotation of [[h00, g01], [g01, g11]] in FP32 from exact inputs
+        const float ddf = narrow_trunc(g11 - h00), g01f = narrow_trunc(g01);
         float cs = 1.0f, sn = 0.0f, tt = 0.0f;
-        if (g01 != 0.0) {
-            const float th = float(g11 - h00) / (2.0f * float(g01));
+        if (g01f != 0.0f) {
+            const float th = ddf / (2.0f * g01f);
             tt = (th >= 0.0f ? 1.0f : -1.0f) / (fabsf(th) + sqrtf(fmaf(th, th, 1.0f)));
             cs = rsqrtf(fmaf(tt, tt, 1.0f));
             sn = tt * cs;
         }
-        const float nU = float(fma(U0, U0, fma(U1, U1, U2 * U2)));
-        const double lxd = fma(-double(tt), g01, h00), lyd = fma(double(tt), g01, g11);
+        const double ttd = widen_f32(tt);
+        const double lxd = fma(-ttd, g01, h00), lyd = fma(ttd, g01, g11);
+        const float nU = fmaf(s1, s1, s2 * s2);                      // |U|^2 = V0
         float lx = float(lxd) / nU, ly = float(lyd) / nU;
-        const float iu = rsqrtf(nU), iv = rsqrtf(float(nw) * nU);
-        float x[3], y[3];
-        const float Vf[3] = {float(V0), float(V1), float(V2)};
+        const float iu = rsqrtf(nU), iv = rsqrtf(fmaf(s0, s0, nU) * nU);
+        const float Ur[3] = {0.0f, -s2, s1}, Vr[3] = {nU, -s0 * s1, -s0 * s2};
+        float xr[3], yr[3];
         for (int i = 0; i < 3; ++i) {
-            const float u = Uf[i] * iu, v = Vf[i] * iv;
-            x[i] = cs * u - sn * v;
-            y[i] = fmaf(sn, u, cs * v);
+            const float u = Ur[i] * iu, v = Vr[i] * iv;
+            xr[i] = cs * u - sn * v;
+            yr[i] = fmaf(sn, u, cs * v);
         }
-        if (lxd > lyd) {   // ordered in FP64: the pair may round to one float
+        // back to the original frame: x[(k + j) % 3] = xr[j]
+        float x[3], y[3];
+        x[0] = k == 0 ? xr[0] : (k == 1 ? xr[2] : xr[1]);
+        x[1] = k == 0 ? xr[1] : (k == 1 ? xr[0] : xr[2]);
+        x[2] = k == 0 ? xr[2] : (k == 1 ? xr[1] : xr[0]);
+        y[0] = k == 0 ? yr[0] : (k == 1 ? yr[2] : yr[1]);
+        y[1] = k == 0 ? yr[1] : (k == 1 ? yr[0] : yr[2]);
+        y[2] = k == 0 ? yr[2] : (k == 1 ? yr[1] : yr[0]);
+        // ly - lx = dd + 2 tt g01, and tt g01 has the sign of dd (of g01 when
+        // dd is 0), so the order follows from signs: no FP64 comparison
+        if (ddf != 0.0f ? ddf < 0.0f : g01f < 0.0f) {
             float tmp;
             for (int i = 0; i < 3; ++i) { tmp = x[i]; x[i] = y[i]; y[i] = tmp; }
             tmp = lx; lx = ly; ly = tmp;
@@ -397,7 +441,7 @@ __device__ __forceinline__ void eig3_precise_fp64(float a, float b, float c, flo
         const float Aw0 = fmaf(Af[0], w[0], fmaf(Af[1], w[1], Af[2] * w[2]));
         const float Aw1 = fmaf(Af[1], w[0], fmaf(Af[3], w[1], Af[4] * w[2]));
         const float Aw2 = fmaf(Af[2], w[0], fmaf(Af[4], w[1], Af[5] * w[2]));
-        const float lw = fmaf(w[0], Aw0, fmaf(w[1], Aw1, w[2] * Aw2)) / float(nw);
+        const float lw = fmaf(w[0], Aw0, fmaf(w[1], Aw1, w[2] * Aw2)) / fmaf(s0, s0, nU);
         assemble<float>(iso_high, lw, w, lx, ly, x, y, ev, v0, v1, v2, unsc);
         return;
     }

@@ -8,7 +8,9 @@
 // stages its tile of AoS records into shared memory with 16-byte coalesced
 // loads, each thread solves one tensor, and results leave through shared
 // memory with 16-byte coalesced stores.  HBM traffic is the algorithmic
-// minimum (read the tensor once, write each output once).
+// minimum (read the tensor once, write each output once).  Each block keeps
+// two input tiles in shared memory: the next tile's copy (cp.async) runs
+// while the current one is solved.
 //
 // Precise mode: a scale-invariant FP32 solve for every tensor; tensors whose
 // remaining pair is closer than 1e-4 |lambda_max| are appended to a compact
@@ -20,6 +22,7 @@
 #include "tvgb_common.cuh"
 #include "eig_device.cuh"
 #include <algorithm>
+#include <mutex>
 
 namespace tvgb {
 
@@ -47,6 +50,17 @@ __device__ __forceinline__ void load_tile(const float* __restrict__ in, size_t n
     }
 }
 
+// The next tile's AoS records copied into shared memory asynchronously
+// (16-byte cp.async per thread, no registers held), so the copy runs while
+// the block solves the current tile.  Full, 16-byte aligned AoS tiles only.
+__device__ __forceinline__ void load_tile_async(const float* __restrict__ src, int nfl, float* s_in) {
+    const uint32_t dst = static_cast<uint32_t>(__cvta_generic_to_shared(s_in));
+    for (int i = threadIdx.x; i < nfl / 4; i += EIG_BLOCK)
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst + 16u * i), "l"(src + 4 * i) : "memory");
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+__device__ __forceinline__ void wait_tile_async() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
 __device__ __forceinline__ void store_tile(float* __restrict__ dst, const float* s, int nfl, bool aligned, bool full) {
     if (aligned && full && (nfl % 4) == 0) {
         float4* d4 = reinterpret_cast<float4*>(dst);
@@ -70,19 +84,33 @@ __global__ void __launch_bounds__(EIG_BLOCK) k_eig3(const float* __restrict__ in
                                                       unsigned* __restrict__ qcount, int aligned_in, int aligned_out) {
     constexpr int NF = IN_LAYOUT == 9 ? 9 : 6;
     constexpr int NV = EVEC_FMT == 1 ? 9 : (EVEC_FMT == 2 ? 6 : 0);
-    __shared__ __align__(16) float s_in[EIG_BLOCK * NF];
+    __shared__ __align__(16) float s_in2[2][EIG_BLOCK * NF];   // the current tile and the next one
     __shared__ __align__(16) float s_ev[EIG_BLOCK * 3];
     __shared__ __align__(16) float s_vec[EIG_BLOCK * 9];
     __shared__ uint4 s_q[PRECISE ? EIG_BLOCK : 1];
     __shared__ unsigned s_qn, s_qbase;
 
-    for (size_t base = first + size_t(blockIdx.x) * EIG_BLOCK; base < last; base += size_t(gridDim.x) * EIG_BLOCK) {
+    const size_t stride = size_t(gridDim.x) * EIG_BLOCK;
+    // tile at `base` into buffer `buf`: asynchronous when full, aligned and AoS
+    auto fetch = [&](size_t base, int buf) {
         const int cnt = int(min(size_t(EIG_BLOCK), last - base));
+        if (IN_LAYOUT != 60 && aligned_in && cnt == EIG_BLOCK)
+            load_tile_async(in + base * NF, EIG_BLOCK * NF, s_in2[buf]);
+        else
+            load_tile<IN_LAYOUT>(in, n, base, cnt, s_in2[buf], aligned_in);
+    };
+    int it = 0;   // tiles done by this block: tile it sits in buffer it & 1
+    if (first + size_t(blockIdx.x) * EIG_BLOCK < last) fetch(first + size_t(blockIdx.x) * EIG_BLOCK, 0);
+    for (size_t base = first + size_t(blockIdx.x) * EIG_BLOCK; base < last; base += stride, ++it) {
+        const int cnt = int(min(size_t(EIG_BLOCK), last - base));
+        const float* s_in = s_in2[it & 1];
         if (PRECISE && threadIdx.x == 0) s_qn = 0;
-        load_tile<IN_LAYOUT>(in, n, base, cnt, s_in, aligned_in);
         if (EVALS_IN)
             for (int i = threadIdx.x; i < cnt * 3; i += EIG_BLOCK) s_ev[i] = __ldg(evals_in + base * 3 + i);
+        wait_tile_async();
         __syncthreads();
+        // the other buffer was last read before the barrier that ended the previous tile
+        if (base + stride < last) fetch(base + stride, (it + 1) & 1);
         const int t = threadIdx.x;
         if (t < cnt) {
             const float* m = s_in + t * NF;
@@ -207,6 +235,42 @@ static int grid_for(size_t items, int per_block) {
     return int(blocks ? blocks : 1);
 }
 
+// Grid of a grid-stride kernel: as many blocks as fit on the GPU at once, so
+// every block is resident from the start and all finish together.  (A grid of
+// a fixed 8 blocks per SM ran k_eig3, 6 resident per SM, in a full wave and a
+// third of a wave.)
+template <class Kernel>
+static int resident_grid(Kernel kern, int block, size_t items) {
+    struct Entry { const void* k; int dev, block, resident; };
+    static std::mutex mu;
+    static Entry cache[32];
+    static int used = 0;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int resident = 0;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        for (int i = 0; i < used; ++i)
+            if (cache[i].k == reinterpret_cast<const void*>(kern) && cache[i].dev == dev && cache[i].block == block)
+                resident = cache[i].resident;
+    }
+    if (resident == 0) {
+        int sms = 152, p = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p, kern, block, 0) != cudaSuccess || p < 1) {
+            cudaGetLastError();
+            p = 1;
+        }
+        resident = sms * p;
+        std::lock_guard<std::mutex> lk(mu);
+        if (used < 32) cache[used++] = Entry{reinterpret_cast<const void*>(kern), dev, block, resident};
+    }
+    size_t blocks = (items + block - 1) / block;
+    const size_t cap = size_t(resident);
+    if (blocks > cap) blocks = cap;
+    return int(blocks ? blocks : 1);
+}
+
 template <int IL, int EF, bool PR, bool EI>
 static int launch_eig3_t(const float* in, size_t n, const float* ev_in, float* ev, float* vec, unsigned long long* nref,
                          cudaStream_t s) {
@@ -214,8 +278,8 @@ static int launch_eig3_t(const float* in, size_t n, const float* ev_in, float* e
     const int ao = (!ev || reinterpret_cast<uintptr_t>(ev) % 16 == 0) && (!vec || reinterpret_cast<uintptr_t>(vec) % 16 == 0);
     if (!PR) {
         KernelTimer kt_("k_eig3", s);
-        k_eig3<IL, EF, PR, EI><<<grid_for(n, EIG_BLOCK), EIG_BLOCK, 0, s>>>(in, n, 0, n, ev_in, ev, vec, nullptr,
-                                                                           nullptr, ai, ao);
+        k_eig3<IL, EF, PR, EI><<<resident_grid(k_eig3<IL, EF, PR, EI>, EIG_BLOCK, n), EIG_BLOCK, 0, s>>>(
+            in, n, 0, n, ev_in, ev, vec, nullptr, nullptr, ai, ao);
         kt_.stop();
         TVGB_LAUNCHED();
         return TVGB_OK;
@@ -231,15 +295,15 @@ static int launch_eig3_t(const float* in, size_t n, const float* ev_in, float* e
         TVGB_CUDA(cudaMemsetAsync(qcount, 0, sizeof(unsigned), s));
         {
             KernelTimer kt_("k_eig3", s);
-            k_eig3<IL, EF, PR, EI><<<grid_for(last - first, EIG_BLOCK), EIG_BLOCK, 0, s>>>(
+            k_eig3<IL, EF, PR, EI><<<resident_grid(k_eig3<IL, EF, PR, EI>, EIG_BLOCK, last - first), EIG_BLOCK, 0, s>>>(
                 in, n, first, last, ev_in, ev, vec, queue, qcount, ai, ao);
             kt_.stop();
         }
         TVGB_LAUNCHED();
         {
             KernelTimer kt_("k_eig3_refine", s);
-            k_eig3_refine<IL, EF><<<grid_for(last - first, 256), 256, 0, s>>>(in, n, first, queue, qcount, ev, vec,
-                                                                            nref);
+            k_eig3_refine<IL, EF><<<resident_grid(k_eig3_refine<IL, EF>, 256, last - first), 256, 0, s>>>(
+                in, n, first, queue, qcount, ev, vec, nref);
             kt_.stop();
         }
         TVGB_LAUNCHED();
