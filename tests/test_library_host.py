@@ -70,3 +70,38 @@ def test_cuda_wrappers_table_matches_reference_numpy_table(tv):
     b = tv.build_neighbors2d(7, 2.0, 0.5, 2, 10)
     for f in a.dtype.names:
         np.testing.assert_allclose(a[f], b[f], rtol=1e-5, atol=1e-6)
+
+
+def test_empty_inputs_give_empty_outputs(tv):
+    """An empty field, volume or batch returns empty outputs; the library
+    returns before it touches a pointer or the GPU."""
+    o, e, v = tv.vote3(np.zeros((0, 4, 4, 3, 3), np.float32), 1.0, w=5, evals=True, evecs="cartesian")
+    assert o.shape == (0, 4, 4, 3, 3) and e.shape == (0, 4, 4, 3) and v.shape == (0, 4, 4, 3, 3)
+    assert tv.structure_tensor3(np.zeros((0, 8, 8), np.float32), 1.0).shape == (6, 0, 8, 8)
+    assert tv.structure_tensor2(np.zeros((0, 5), np.float32), 1.0).shape == (0, 5, 4)
+    o, e, v = tv.pipeline3(np.zeros((0, 8, 8), np.float32), 1.0, 2.0, w=5)
+    assert o.shape == (6, 0, 8, 8) and e.shape == (0, 8, 8, 3) and v.shape == (0, 8, 8, 3, 3)
+    e, v, nref = tv.eig3(np.zeros((0, 9), np.float32))
+    assert e.shape == (0, 3) and v.shape == (0, 3, 3) and nref == 0
+    assert tv.evals3_symmetric(np.zeros((0, 9), np.float32)).shape == (0, 3)
+    assert tv.evals2_symmetric(np.zeros((0, 4), np.float32)).shape == (0, 2)
+    out = np.zeros((0, 5, 4), np.float32)
+    tv.tensorvote(out, np.zeros((0, 5, 4), np.float32), 1.0, 0.0, 1, 5, 0, 5)
+
+
+def test_inputs_smaller_than_the_window_raise(tv):
+    """A valid convolution of an input smaller than its window is refused by
+    the library with its own message (argument checks run before any GPU
+    work)."""
+    cases = [
+        (lambda: tv.gaussian_convolve2(np.zeros((3, 6), np.float32), 1.0), "smaller than the window"),
+        (lambda: tv.gaussian_filter3d(np.zeros((4, 20, 20), np.float32)), "smaller than the window"),
+        (lambda: tv.structure_tensor3(np.zeros((4, 20, 20), np.float32), 1.0, mode="valid"), "smaller than"),
+        (lambda: tv.structure_tensor2(np.zeros((3, 20), np.float32), 1.0, mode="valid"), "smaller than"),
+        (lambda: tv.pipeline3(np.zeros((4, 20, 20), np.float32), 1.0, 2.0, w=5, st_mode="valid"), "smaller than"),
+    ]
+    for fn, msg in cases:
+        with pytest.raises(tv.TvgbError, match=msg):
+            fn()
+    with pytest.raises(tv.TvgbError, match="must be odd"):
+        tv.vote3(np.zeros((0, 4, 4, 3, 3), np.float32), 1.0, w=4)   # arguments are checked even when empty

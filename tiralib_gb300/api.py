@@ -168,7 +168,7 @@ def gaussian_filter3d(source, width=None, height=None, depth=None, sigma_w=1.0, 
         depth, height, width = source.shape
     dims = (ctypes.c_uint * 3)()
     k = [int(np.ceil(np.float32(6.0) * np.float32(s))) | 1 for s in (sigma_w, sigma_h, sigma_d)]
-    out = _empty_like_kind(source, (depth - k[2] + 1, height - k[1] + 1, width - k[0] + 1))
+    out = _empty_like_kind(source, _valid(depth - k[2] + 1, height - k[1] + 1, width - k[0] + 1))
     call("tvgb_gaussian_filter3d", _ptr(source), width, height, depth, sigma_w, sigma_h, sigma_d, _ptr(out),
          dims, _stream_for(source))
     return out
@@ -181,10 +181,16 @@ def gaussian_convolve2(source, sigma1, sigma2=None):
     sigma2 = sigma1 if sigma2 is None else sigma2
     sy, sx = source.shape
     kw, kh = int(np.float32(6.0) * np.float32(sigma1)), int(np.float32(6.0) * np.float32(sigma2))
-    out = _empty_like_kind(source, (sy - kh + 1, sx - kw + 1))
+    out = _empty_like_kind(source, _valid(sy - kh + 1, sx - kw + 1))
     dims = (ctypes.c_uint * 2)()
     call("tvgb_gaussian_convolve2", _ptr(source), sx, sy, sigma1, sigma2, _ptr(out), dims, _stream_for(source))
     return out
+
+
+def _valid(*dims):
+    """Output extent of a valid convolution, clamped at 0 so that an input
+    smaller than the window reaches the library, which reports it."""
+    return tuple(max(int(d), 0) for d in dims)
 
 
 def _ksize3(sigma):
@@ -200,7 +206,7 @@ def structure_tensor3(volume, sigma, mode="same", layout="planes"):
     s0, s1, s2 = volume.shape
     m = 0 if mode == "valid" else 1
     K = _ksize3(sigma)
-    d = (s0 - K + 1, s1 - K + 1, s2 - K + 1) if m == 0 else (s0, s1, s2)
+    d = _valid(s0 - K + 1, s1 - K + 1, s2 - K + 1) if m == 0 else (s0, s1, s2)
     L = LAYOUTS[layout]
     shape = (6,) + d if L == LAYOUT_SYM6_PLANES else (d + (6,) if L == LAYOUT_SYM6 else d + (3, 3))
     out = _empty_like_kind(volume, shape)
@@ -216,7 +222,7 @@ def structure_tensor2(image, sigma, mode="same"):
     s0, s1 = image.shape
     m = 0 if mode == "valid" else 1
     K = int(np.float32(6.0) * np.float32(sigma))
-    d = (s0 - K + 1, s1 - K + 1) if m == 0 else (s0, s1)
+    d = _valid(s0 - K + 1, s1 - K + 1) if m == 0 else (s0, s1)
     out = _empty_like_kind(image, d + (4,))
     dims = (ctypes.c_uint * 2)()
     call("tvgb_structure_tensor2", _ptr(image), s0, s1, sigma, m, _ptr(out), dims, _stream_for(image))
@@ -311,7 +317,7 @@ def pipeline3(volume, sigma_st, sigma1, sigma2=0.0, w=0, power=1, samples=20, st
     s0, s1, s2 = volume.shape
     m = 0 if st_mode == "valid" else 1
     K = _ksize3(sigma_st)
-    dims = (s0 - K + 1, s1 - K + 1, s2 - K + 1) if m == 0 else (s0, s1, s2)
+    dims = _valid(s0 - K + 1, s1 - K + 1, s2 - K + 1) if m == 0 else (s0, s1, s2)
     OL = LAYOUTS[out_layout]
     fmt = EVECS[evecs]
     if outputs is None:
