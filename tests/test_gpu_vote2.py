@@ -79,15 +79,3 @@ def test_tk_ragged_sizes_against_oracle(mods):
         out = tk.tensorvote_tk(F, 3.0, 0.5, 2, 0, True, True, 20)
         ref = O.tensorvote2(F, 3.0, 0.5, 2, 19, samples=20)
         assert rel(out, ref) < 1e-4
-
-
-def test_validation_messages(mods):
-    tk, atv, _ = mods
-    with pytest.raises(RuntimeError, match=r"shape \(H, W, 4\)"):
-        tk.tensorvote_tk(np.zeros((4, 4, 3), np.float32), 1.0)
-    with pytest.raises(RuntimeError, match="sigma1 must be > 0"):
-        tk.tensorvote_tk(np.zeros((4, 4, 4), np.float32), 0.0)
-    with pytest.raises(RuntimeError, match="sigma must be > 0"):
-        atv.tensorvote_atv(np.zeros((4, 4, 4), np.float32), 0.0)
-    with pytest.raises(RuntimeError, match="positive odd"):
-        tk.tensorvote_tk_prebuilt(np.zeros((4, 4, 4), np.float32), b"", 0, 4, 1.0)
