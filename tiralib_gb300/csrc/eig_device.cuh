@@ -359,7 +359,8 @@ __device__ __forceinline__ float narrow_trunc(double x) {
 // off-diagonal, which cancel for a close pair, are exact to FP64 rounding.
 // The Jacobi angle needs only FP32 relative accuracy from those two numbers,
 // the pair's eigenvalues come from the rotated FP64 diagonal, and the frame
-// is completed in FP32.  41 FP64 operations in all.
+// is completed in FP32.  41 FP64 arithmetic operations, and two conversions
+// (the pair's eigenvalues to FP32).
 // code 2: cyclic Jacobi on the whole matrix in FP64.
 __device__ __forceinline__ void eig3_precise_fp64(float a, float b, float c, float d, float e, float f, const float* w,
                                                   bool iso_high, int code, float* ev, float* v0, float* v1, float* v2) {
