@@ -1,0 +1,175 @@
+"""Parity at the full sizes of the benchmark configurations, where the CPU
+oracle cannot vote every receiver.
+
+Over the whole field or batch, properties that hold at any size:
+- exact power-of-two scaling in precise mode: pipeline3(2 v) = 4 pipeline3(v)
+  and eig3(2 M) = 2 eig3(M) bit for bit, with identical eigenvectors.  Every
+  step is homogeneous (gradients, products, blurs, votes), the precise
+  eigensolver scales each tensor by a power of two first, and a power of two
+  commutes with every rounding.  (Parity mode keeps eigen.h's absolute
+  thresholds, which are not scale-free.)
+- votes of positive semi-definite voters are positive semi-definite, and the
+  fused eigenvalues come out ascending.
+On a sample of receivers, agreement with the reference's CPU algorithm (the
+oracle: its own structure tensor, stick + 20-sample plate) within the parity
+bar 1e-4, and of precise mode with the FP64 oracle.  The 2D configuration is
+small enough to check every pixel against the oracle.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import bench
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+THREADS = os.cpu_count() or 1
+WGT = np.array([1, 2, 2, 1, 2, 1], np.float64)   # off-diagonal entries count twice in the Frobenius norm
+
+
+@pytest.fixture(scope="module")
+def torch_dev():
+    import torch
+    return torch, torch.device("cuda", 0)
+
+
+def tensor_rel(a, ref):
+    """Per receiver ||a - ref|| / ||ref|| over the six unique entries."""
+    return np.sqrt((WGT * (a - ref) ** 2).sum(1) / np.maximum((WGT * ref ** 2).sum(1), 1e-300))
+
+
+def run3(tv, vol, cfg, parity):
+    return tv.pipeline3(vol, cfg["sigma_st"], cfg["sigma"], w=cfg["w"], samples=cfg["samples"], ball=cfg["ball"],
+                        parity=parity, out_layout="planes", evals=True, evecs="cartesian")
+
+
+def at_block(detail, out, ev, vec):
+    z0, y0, x0, b = detail["block"]
+    sl = (slice(z0, z0 + b), slice(y0, y0 + b), slice(x0, x0 + b))
+    g6 = np.moveaxis(out[(slice(None),) + sl].cpu().numpy(), 0, -1).reshape(-1, 6).astype(np.float64)
+    return g6, ev[sl].cpu().numpy().reshape(-1, 3).astype(np.float64), vec[sl].cpu().numpy().reshape(-1, 3, 3)
+
+
+def check_field_properties(torch, out, ev, vec):
+    lam = ev.reshape(-1, 3)
+    assert bool((lam[:, 0] <= lam[:, 1]).all()) and bool((lam[:, 1] <= lam[:, 2]).all())
+    scale = lam.abs().amax(dim=1).clamp_min(1e-30)
+    assert float((lam[:, 0] / scale).min()) > -1e-5                       # positive semi-definite votes
+    # a sample of voxels: the eigenpairs reconstruct the voted tensor, the frame is orthonormal
+    n = lam.shape[0]
+    idx = torch.randperm(n, device=lam.device, generator=torch.Generator(device=lam.device).manual_seed(5))[:1 << 16]
+    V = vec.reshape(-1, 3, 3)[idx].double()                               # rows e0, e1, e2
+    L = lam[idx].double()
+    R = torch.einsum("nki,nk,nkj->nij", V, L, V)
+    T6 = out.reshape(6, -1)[:, idx].t().double()
+    T = torch.stack([T6[:, 0], T6[:, 1], T6[:, 2], T6[:, 1], T6[:, 3], T6[:, 4], T6[:, 2], T6[:, 4], T6[:, 5]],
+                    dim=1).view(-1, 3, 3)
+    back = (R - T).flatten(1).norm(dim=1) / T.flatten(1).norm(dim=1).clamp_min(1e-300)
+    assert float(back.max()) < 1e-5
+    eye = torch.eye(3, dtype=torch.float64, device=V.device)
+    assert float((V @ V.transpose(1, 2) - eye).abs().max()) < 1e-5
+
+
+@pytest.mark.parametrize("name", ["c2", "c4"])
+def test_tube_field_at_full_size(torch_dev, name):
+    """C2 (256^3) and C4 (384^3), sigma 4, w 25: the whole field's properties,
+    exact scaling, and a 4^3 receiver sample against the reference's CPU
+    algorithm."""
+    torch, dev = torch_dev
+    import tiralib_gb300 as tv
+    cfg = dict(bench.CONFIGS3[name])
+    vol = bench.make_volume(cfg, dev)
+    vol_d = vol if torch.is_tensor(vol) else torch.from_numpy(vol).to(dev)
+    out, ev, vec = run3(tv, vol_d, cfg, parity=True)
+    torch.cuda.synchronize()
+    # the reference's CPU algorithm (parity mode) on a sample of receivers
+    detail = {}
+    bench.cpu_reference_sample(vol_d.cpu().numpy(), cfg, block=4, seed=7, threads=THREADS, detail=detail)
+    g6, gev, gvec = at_block(detail, out, ev, vec)
+    c6 = detail["voted"].reshape(-1, 9)[:, [0, 1, 2, 4, 5, 8]].astype(np.float64)
+    assert tensor_rel(g6, c6).max() < 1e-4
+    cev = detail["evals"].astype(np.float64)
+    assert (np.abs(gev - cev).max(1) / np.abs(cev).max(1)).max() < 1e-4
+    del out, ev, vec
+    # precise mode: the whole field's properties, and exact power-of-two scaling of the whole pipeline
+    p1 = run3(tv, vol_d, cfg, parity=False)
+    torch.cuda.synchronize()
+    check_field_properties(torch, *p1)
+    p2 = run3(tv, 2.0 * vol_d, cfg, parity=False)
+    torch.cuda.synchronize()
+    assert torch.equal(p2[0], 4.0 * p1[0])
+    assert torch.equal(p2[1], 4.0 * p1[1])
+    assert torch.equal(p2[2], p1[2])
+
+
+def test_capacity_field_with_ball_at_full_size(torch_dev):
+    """C5 (512^3 tubes and sheets, sigma 6, w 37, stick + plate + ball) in
+    precise mode: the whole field's properties and a 4^3 receiver sample
+    against the FP64 oracle (the reference has no TK ball term)."""
+    torch, dev = torch_dev
+    import tiralib_gb300 as tv
+    cfg = dict(bench.CONFIGS3["c5"])
+    vol = bench.make_volume(cfg, dev)
+    out, ev, vec = run3(tv, vol, cfg, parity=False)
+    torch.cuda.synchronize()
+    check_field_properties(torch, out, ev, vec)
+    detail = {}
+    bench.cpu_reference_sample(vol.cpu().numpy(), cfg, block=4, seed=7, threads=THREADS, detail=detail)
+    g6, gev, _ = at_block(detail, out, ev, vec)
+    f64 = O.tensorvote3_f64(detail["field"], cfg["sigma"], 0.0, cfg["w"], 1, ball=True,
+                            receivers=detail["receivers"], threads=THREADS).reshape(-1, 6)[detail["receivers"]]
+    assert tensor_rel(g6, f64).max() < 1e-5
+    fev, _ = O.eig3_f64(f64)
+    assert (np.abs(gev - fev).max(1) / np.abs(fev).max(1)).max() < 1e-5
+
+
+def test_eigen_batch_at_full_size(torch_dev):
+    """C3: 2^27 tensors of the precision recipe in precise mode.  Exact
+    scaling over the whole batch; ascending eigenvalues; on a 2^16 sample,
+    eigenvalues against FP64 Jacobi within 2e-6 of |lambda_max| and the
+    eigenvectors of well-separated eigenvalues within 1e-4 rad."""
+    torch, dev = torch_dev
+    import tiralib_gb300 as tv
+    n = 1 << 27
+    M = bench.eigen_batch_gpu(n, 3, dev)
+    ev, vec, nref = tv.eig3(M, precise=True)
+    ev2, vec2, _ = tv.eig3(2.0 * M, precise=True)
+    torch.cuda.synchronize()
+    assert nref > 0
+    assert torch.equal(ev2, 2.0 * ev) and torch.equal(vec2, vec)
+    assert bool((ev[:, 0] <= ev[:, 1]).all()) and bool((ev[:, 1] <= ev[:, 2]).all())
+    idx = torch.randperm(n, device=dev, generator=torch.Generator(device=dev).manual_seed(9))[:1 << 16]
+    m9 = M[idx].cpu().numpy().astype(np.float64)
+    fev, fvec = O.eig3_f64(m9[:, [0, 1, 2, 4, 5, 8]])
+    gev = ev[idx].cpu().numpy().astype(np.float64)
+    gvec = vec[idx].cpu().numpy().astype(np.float64)
+    scale = np.abs(fev).max(1)
+    assert (np.abs(gev - fev).max(1) / scale).max() < 2e-6
+    gap = np.minimum(fev[:, 1] - fev[:, 0], fev[:, 2] - fev[:, 1]) / scale
+    sep = gap > 1e-2
+    # angle as atan2(|u x v|, |u . v|) of the normalised vectors: an FP32 vector's norm is 1 only to ~1e-7,
+    # which arccos of the dot product would turn into a spurious 3e-4 rad
+    u = gvec[sep] / np.linalg.norm(gvec[sep], axis=2, keepdims=True)
+    ang = np.arctan2(np.linalg.norm(np.cross(u, fvec[sep]), axis=2), np.abs((u * fvec[sep]).sum(2)))
+    assert sep.sum() > (1 << 14) and ang.max() < 1e-4
+
+
+def test_2d_image_at_full_size_every_pixel():
+    """C1 (512^2 curve image, sigma 3, w 19, 20 plate samples): the structure
+    tensor and the vote of every pixel against the oracle, and the eigenpairs
+    against the oracle's eigen.h restatement."""
+    import tiralib_gb300 as tv
+    from tiralib_gb300 import workloads as W
+    img = W.curve_image(512, seed=1)
+    st = tv.structure_tensor2(img, 1.0)
+    st_ref = O.structure_tensor2(img, 1.0, 1)
+    assert np.abs(st - st_ref).max() / np.abs(st_ref).max() < 1e-5
+    voted = np.zeros_like(st)
+    tv.tensorvote(voted, st, 3.0, 0.0, 1, 19, 512, 512, True, True, 20)
+    ref = O.tensorvote2(st, 3.0, 0.0, 1, 19, samples=20)
+    assert np.abs(voted - ref).max() / np.abs(ref).max() < 1e-4
+    ev = tv.evals2_symmetric(voted)
+    ev_ref = O.evals2(ref)
+    assert np.abs(ev - ev_ref).max() / np.abs(ev_ref).max() < 1e-4
