@@ -1,6 +1,8 @@
-"""The benchmark's reference arm, run on the CPU with a small volume and a
-small receiver sample: its JSON line keeps the keys and units of the
-benchmark contract, and under a multi-rank launch only rank 0 prints."""
+"""The benchmark's host side on the CPU.  The reference arm, run with a small
+volume and a small receiver sample, keeps the keys and units of the
+benchmark contract in its JSON line, and under a multi-rank launch only rank
+0 prints.  The roofline's pair count is exact, and the kernel summaries the
+bench reads its DRAM traffic from carry that figure."""
 import json
 import os
 import subprocess
@@ -46,3 +48,32 @@ def test_reference_arm_runs_on_rank_0_only():
     r = _run({"RANK": "1", "WORLD_SIZE": "2", "LOCAL_RANK": "1"})
     assert r.returncode == 0, r.stderr[-2000:]
     assert _json_lines(r.stdout) == []
+
+
+def test_pair_count_is_exact():
+    """The roofline's algorithmic work counts in-bounds (receiver, voter)
+    pairs exactly: against brute force on small volumes, and on a z-slab."""
+    import numpy as np
+    import bench
+    for dims, hw in [((5, 7, 9), 2), ((3, 4, 20), 5), ((1, 1, 1), 3), ((6, 6, 6), 0)]:
+        s0, s1, s2 = dims
+        z, y, x = np.meshgrid(np.arange(s0), np.arange(s1), np.arange(s2), indexing="ij")
+        brute = 0
+        for oz in range(-hw, hw + 1):
+            for oy in range(-hw, hw + 1):
+                for ox in range(-hw, hw + 1):
+                    brute += int(((z + oz >= 0) & (z + oz < s0) & (y + oy >= 0) & (y + oy < s1) &
+                                  (x + ox >= 0) & (x + ox < s2)).sum())
+        assert bench.pairs_count(dims, hw) == brute
+    full = bench.pairs_count((12, 5, 5), 3)
+    assert bench.pairs_count((12, 5, 5), 3, (0, 4)) + bench.pairs_count((12, 5, 5), 3, (4, 12)) == full
+
+
+def test_profiles_carry_the_traffic_the_bench_reads():
+    """Every kernel summary the bench takes its DRAM traffic from keeps a
+    machine-readable per-launch figure."""
+    import bench
+    for kernel, workload in [("k_vote3_fast", "c2"), ("k_vote3_fast", "c4"), ("k_eig3", "c3"),
+                             ("k_vote2_tk", "c1"), ("k_st3", "c2")]:
+        t = bench.profiled_traffic(kernel, workload)
+        assert t is not None and t > 0, (kernel, workload)
