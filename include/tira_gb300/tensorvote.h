@@ -12,6 +12,9 @@
 //   * the eigen / filter functions return newly allocated arrays, new[] /
 //     malloc for host input and cudaMalloc for device input, as the reference
 //     (eigen.h:933-941, 996-1006; filter.h:518-526); the caller frees them;
+//   * a negative device index, which the reference's eigen launchers send to
+//     their CPU code (eigen.h:897,946), is an error here: this library has no
+//     CPU path.  Those calls report it and return nullptr;
 //   * errors are printed and execution continues, as HANDLE_ERROR does
 //     (tira/cuda/error.h:11-15); define TIRA_GB300_THROW to throw
 //     std::runtime_error instead.
@@ -25,6 +28,7 @@
 #include <stdexcept>
 #include <string>
 #include <type_traits>
+#include <vector>
 #include <cuda_runtime.h>
 
 #include "../tvgb.h"
@@ -38,6 +42,33 @@ inline void check(int status, const char* fn) {
 #else
     std::printf("%s failed: %s\n", fn, tvgb_last_error());
 #endif
+}
+
+// Reports a failure the way check() does, for errors found in the shim itself.
+inline void fail(const char* fn, const std::string& what) {
+#ifdef TIRA_GB300_THROW
+    throw std::runtime_error(std::string(fn) + ": " + what);
+#else
+    std::printf("%s failed: %s\n", fn, what.c_str());
+#endif
+}
+
+// The reference's eigen launchers take a device index and run on the CPU
+// when it is negative (eigen.h:897,946).  This library has no CPU path, so a
+// negative index is an error, and so is a device that cannot be made current.
+inline bool select_device(int device, const char* fn) {
+    if (device < 0) {
+        fail(fn, "device " + std::to_string(device) +
+                     " requests the reference's CPU path, which this GPU library does not provide");
+        return false;
+    }
+    const cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        fail(fn, "cudaSetDevice(" + std::to_string(device) + "): " + cudaGetErrorString(e));
+        return false;
+    }
+    return true;
 }
 
 inline bool on_device(const void* p) {
@@ -75,14 +106,51 @@ struct Neighbor2D {
 };
 static_assert(sizeof(Neighbor2D) == 48, "Neighbor2D must be 48 bytes");
 
+// tira::Neighbor3D (tensorvote.h:1147), byte-compatible.  The reference's d
+// is a glm::vec3; here it is a plain three-float struct with the same
+// layout (x, y, z), so the shim does not need glm.
+struct Neighbor3D {
+    struct vec3 {
+        float x, y, z;
+        float& operator[](int i) { return (&x)[i]; }
+        const float& operator[](int i) const { return (&x)[i]; }
+    };
+    int du, dv, dw;   // offsets along x2 (fast), x1, x0 (slow)
+    vec3 d;           // unit direction of (du, dv, dw); zero at the centre
+    float c1, c2;     // exp(-l2 / sigma1^2), exp(-l2 / sigma2^2)
+};
+static_assert(sizeof(Neighbor3D) == 32, "Neighbor3D must be 32 bytes");
+
 namespace cpu {
-// tira::cpu::build_neighbors2d (tensorvote.h:1223)
-inline std::size_t build_neighbors2d(int w, float sigma1, float sigma2, unsigned power, unsigned samples, bool stick,
-                                     bool plate, Neighbor2D* out) {
+// tira::cpu::build_neighbors2d (tensorvote.h:1222-1223): the w*w table, as a vector
+inline std::vector<Neighbor2D> build_neighbors2d(const int w, const float sigma1, const float sigma2,
+                                                 const unsigned power, const unsigned samples, const bool stick,
+                                                 const bool plate) {
+    std::vector<Neighbor2D> nb;
     int count = 0;
-    tira_gb300::check(tvgb_build_neighbors2d(w, sigma1, sigma2, power, samples, stick, plate, out, &count),
-                      "build_neighbors2d");
-    return std::size_t(count);
+    const int st = tvgb_build_neighbors2d(w, sigma1, sigma2, power, samples, stick, plate, nullptr, &count);
+    tira_gb300::check(st, "tira::cpu::build_neighbors2d");
+    if (st != TVGB_OK || count <= 0) return nb;
+    nb.resize(std::size_t(count));
+    tira_gb300::check(tvgb_build_neighbors2d(w, sigma1, sigma2, power, samples, stick, plate, nb.data(), &count),
+                      "tira::cpu::build_neighbors2d");
+    return nb;
+}
+
+// tira::cpu::build_neighbors3d (tensorvote.h:1411): the w*w*w table.  sigma is
+// any (x, y) pair type, e.g. glm::vec2 as in the reference, read as
+// (sigma1, sigma2).
+template <class Vec2>
+inline std::vector<Neighbor3D> build_neighbors3d(int w, Vec2 sigma) {
+    std::vector<Neighbor3D> nb;
+    int count = 0;
+    const int st = tvgb_build_neighbors3d(w, float(sigma.x), float(sigma.y), nullptr, &count);
+    tira_gb300::check(st, "tira::cpu::build_neighbors3d");
+    if (st != TVGB_OK || count <= 0) return nb;
+    nb.resize(std::size_t(count));
+    tira_gb300::check(tvgb_build_neighbors3d(w, float(sigma.x), float(sigma.y), nb.data(), &count),
+                      "tira::cpu::build_neighbors3d");
+    return nb;
 }
 }  // namespace cpu
 
@@ -126,7 +194,7 @@ void tensorvote_prebuilt(Type* t_out, const Type* t_in, const Neighbor2D* host_n
 // tira::cuda::evals3_symmetric (eigen.h:896): returns a new (3 n) array
 template <class Type, tira_gb300::only_float<Type> = 0>
 Type* evals3_symmetric(const Type* mats, const size_t n, int device) {
-    cudaSetDevice(device);
+    if (!tira_gb300::select_device(device, "tira::cuda::evals3_symmetric")) return nullptr;
     Type* out = tira_gb300::alloc_like<Type>(mats, 3 * n);
     tira_gb300::check(tvgb_evals3_symmetric(mats, n, out, nullptr), "tira::cuda::evals3_symmetric");
     cudaDeviceSynchronize();
@@ -137,7 +205,7 @@ Type* evals3_symmetric(const Type* mats, const size_t n, int device) {
 // array, on the device if either input is device memory
 template <class Type, tira_gb300::only_float<Type> = 0>
 Type* evecs3spherical_symmetric(const Type* mats, const Type* lambda, const size_t n, int device) {
-    cudaSetDevice(device);
+    if (!tira_gb300::select_device(device, "tira::cuda::evecs3spherical_symmetric")) return nullptr;
     const void* ref = tira_gb300::on_device(mats) ? static_cast<const void*>(mats) : static_cast<const void*>(lambda);
     Type* out = tira_gb300::alloc_like<Type>(ref, 6 * n);
     tira_gb300::check(tvgb_evecs3spherical_symmetric(mats, lambda, n, out, nullptr),
@@ -149,7 +217,7 @@ Type* evecs3spherical_symmetric(const Type* mats, const Type* lambda, const size
 // tira::cuda::evals2_symmetric (eigen.h:769)
 template <class Type, tira_gb300::only_float<Type> = 0>
 Type* evals2_symmetric(const Type* mats, const size_t n, int device) {
-    cudaSetDevice(device);
+    if (!tira_gb300::select_device(device, "tira::cuda::evals2_symmetric")) return nullptr;
     Type* out = tira_gb300::alloc_like<Type>(mats, 2 * n);
     tira_gb300::check(tvgb_evals2_symmetric(mats, n, out, nullptr), "tira::cuda::evals2_symmetric");
     cudaDeviceSynchronize();
@@ -159,7 +227,7 @@ Type* evals2_symmetric(const Type* mats, const size_t n, int device) {
 // tira::cuda::evecs2polar_symmetric (eigen.h:828)
 template <class Type, tira_gb300::only_float<Type> = 0>
 Type* evecs2polar_symmetric(const Type* mats, const Type* evals, size_t n, int device) {
-    cudaSetDevice(device);
+    if (!tira_gb300::select_device(device, "tira::cuda::evecs2polar_symmetric")) return nullptr;
     const void* ref = tira_gb300::on_device(mats) ? static_cast<const void*>(mats) : static_cast<const void*>(evals);
     Type* out = tira_gb300::alloc_like<Type>(ref, 2 * n);
     tira_gb300::check(tvgb_evecs2polar_symmetric(mats, evals, n, out, nullptr), "tira::cuda::evecs2polar_symmetric");

@@ -132,6 +132,9 @@ int tvgb_structure_tensor2(const float* image, unsigned s0, unsigned s1, float s
  * form whenever samples >= power + 2); ATV (tensorvote.h:2640) when is_atv
  * != 0, with sigma as the ATV sigma.  The output is symmetric (the reference
  * GPU kernels write both halves, tensorvote.h:2452-2454, 2630-2632). */
+/* device must be >= 0 and is made current (the reference's negative index
+ * selects its CPU eigen path, eigen.h:897, which is not provided): a
+ * negative index returns TVGB_ERR_ARG. */
 int tvgb_tensorvote3(const float* input_field, float* output_field, unsigned s0, unsigned s1, unsigned s2,
                      float sigma, float sigma2, unsigned w, unsigned power, int device, int stick, int plate,
                      unsigned samples, int is_atv, void* stream);
@@ -153,6 +156,12 @@ int tvgb_tensorvote_prebuilt(float* t_out, const float* t_in, const void* host_n
  * w*w Neighbor2D records to out (may be NULL) and their count to count. */
 int tvgb_build_neighbors2d(int w, float sigma1, float sigma2, unsigned power, unsigned samples, int stick,
                            int plate, void* out, int* count);
+
+/* Replaces tira::cpu::build_neighbors3d (tensorvote.h:1411), host only: writes
+ * w*w*w tira::Neighbor3D records (tensorvote.h:1147; 32 bytes each: int32
+ * du, dv, dw, float32 d.x, d.y, d.z, c1, c2) to out (may be NULL) and their
+ * count to count. */
+int tvgb_build_neighbors3d(int w, float sigma1, float sigma2, void* out, int* count);
 
 /* Extended 3D voting (no single reference function; the options below extend
  * tira::cuda::tensorvote3, tensorvote.h:2817). */

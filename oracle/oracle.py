@@ -89,6 +89,8 @@ _REF_SIGS = {
     "ref_gaussian_convolve2": (None, [_P, _U, _U, _F, _P, _P]),
     "ref_build_neighbors2d": (_I, [_I, _F, _F, _U, _U, _I, _I, _P]),
     "ref_sizeof_neighbor2d": (_I, []),
+    "ref_build_neighbors3d": (_I, [_I, _F, _F, _P]),
+    "ref_sizeof_neighbor3d": (_I, []),
     "ref_tensorvote2": (None, [_P, _P, _F, _F, _I, _U, _U, _U, _I, _I, _U, _I]),
     "ref_tensorvote3": (None, [_P, _P, _U, _U, _U, _F, _F, _U, _U, _I, _I, _U, _I]),
     "ref_sticknorm3": (_D, [_F, _F, _U]),
@@ -291,11 +293,25 @@ NB2_DTYPE = np.dtype([
     ("Va", np.float32), ("Vb", np.float32), ("Vc", np.float32),
 ])
 
+NB3_DTYPE = np.dtype([
+    ("du", np.int32), ("dv", np.int32), ("dw", np.int32),
+    ("d", np.float32, (3,)),
+    ("c1", np.float32), ("c2", np.float32),
+])
+
 
 def build_neighbors2d(w, s1, s2, power, samples, stick=True, plate=True, use_ref=False):
     out = np.zeros(w * w, NB2_DTYPE)
     fn = ref().ref_build_neighbors2d if use_ref else lib().or_build_neighbors2d
     n = fn(w, s1, s2, power, samples, int(stick), int(plate), _ptr(out))
+    return out[:n]
+
+
+def build_neighbors3d_ref(w, s1, s2):
+    """The compiled reference's tira::cpu::build_neighbors3d table (fixtures only)."""
+    assert ref().ref_sizeof_neighbor3d() == NB3_DTYPE.itemsize
+    out = np.zeros(w ** 3, NB3_DTYPE)
+    n = ref().ref_build_neighbors3d(w, s1, s2, _ptr(out))
     return out[:n]
 
 

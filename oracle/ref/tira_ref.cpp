@@ -95,6 +95,15 @@ int ref_build_neighbors2d(int w, float sigma1, float sigma2, unsigned power, uns
 
 int ref_sizeof_neighbor2d(void) { return int(sizeof(tira::Neighbor2D)); }
 
+// Writes count * 32 bytes (tira::Neighbor3D) into out; returns the count.
+int ref_build_neighbors3d(int w, float sigma1, float sigma2, void* out) {
+    std::vector<tira::Neighbor3D> nb = tira::cpu::build_neighbors3d(w, glm::vec2(sigma1, sigma2));
+    if (out) std::memcpy(out, nb.data(), nb.size() * sizeof(tira::Neighbor3D));
+    return int(nb.size());
+}
+
+int ref_sizeof_neighbor3d(void) { return int(sizeof(tira::Neighbor3D)); }
+
 void ref_tensorvote2(float* out4, const float* in4, float sigma1, float sigma2, int power, unsigned w,
                      unsigned s0, unsigned s1, int stick, int plate, unsigned samples, int is_atv) {
     tira::cpu::tensorvote<float>(out4, in4, sigma1, sigma2, power, w, s0, s1,

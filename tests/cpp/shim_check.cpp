@@ -4,11 +4,14 @@
 // eigenvalues through tira::cuda::evals3_symmetric and blurs a volume with
 // tira::cuda::gaussian_filter3d, all with host pointers, and writes the raw
 // results to the file named on the command line (checked by
-// tests/test_gpu_shim.py against the CPU oracle).
+// tests/test_gpu_shim.py against the CPU oracle).  With --host it only
+// builds the neighbour tables and checks the negative-device rule, which
+// needs no GPU (tests/test_shim_build.py).
 #include <tira_gb300/tensorvote.h>
 
 #include <cstdint>
 #include <cstdio>
+#include <string>
 #include <vector>
 
 static float lcg(uint64_t& s) {
@@ -16,11 +19,36 @@ static float lcg(uint64_t& s) {
     return float((s >> 40) & 0xFFFFFF) / float(0x1000000) * 2.0f - 1.0f;
 }
 
+// glm::vec2 stand-in: the reference passes the 3D sigmas as a glm::vec2.
+struct sigma_pair {
+    float x, y;
+};
+
+// Host-only part (no GPU needed): the neighbour tables in the reference's
+// calling form, and the eigen launcher's answer to a negative device index.
+static int host_part(const char* path) {
+    std::vector<tira::Neighbor2D> nb2 = tira::cpu::build_neighbors2d(7, 2.0f, 0.5f, 2, 10, true, true);
+    auto nb3 = tira::cpu::build_neighbors3d(7, sigma_pair{2.0f, 0.5f});
+    const float m9[9] = {2, 0, 0, 0, 1, 0, 0, 0, 3};
+    float* ev = tira::cuda::evals3_symmetric<float>(m9, 1, -1);   // the reference would use its CPU path
+    const int32_t counts[3] = {int32_t(nb2.size()), int32_t(nb3.size()), ev == nullptr ? 1 : 0};
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return 3;
+    std::fwrite(counts, sizeof(int32_t), 3, f);
+    std::fwrite(nb2.data(), sizeof(tira::Neighbor2D), nb2.size(), f);
+    std::fwrite(nb3.data(), sizeof(tira::Neighbor3D), nb3.size(), f);
+    std::fclose(f);
+    delete[] ev;
+    std::printf("host ok %zu %zu\n", nb2.size(), nb3.size());
+    return 0;
+}
+
 int main(int argc, char** argv) {
     if (argc < 2) {
-        std::fprintf(stderr, "usage: %s <out.bin>\n", argv[0]);
+        std::fprintf(stderr, "usage: %s [--host] <out.bin>\n", argv[0]);
         return 2;
     }
+    if (std::string(argv[1]) == "--host") return argc > 2 ? host_part(argv[2]) : 2;
     const unsigned s0 = 6, s1 = 7, s2 = 8;
     const size_t n = size_t(s0) * s1 * s2;
     std::vector<float> in(9 * n), out(9 * n, 0.0f);

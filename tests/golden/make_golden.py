@@ -2,7 +2,10 @@
 
 Run in a checkout where the tiralib reference tree is available:
 
-    python tests/golden/make_golden.py <path to the tiralib checkout>
+    python tests/golden/make_golden.py [<path to the tiralib checkout> [nb3]]
+
+The path defaults to $TIRALIB_REFERENCE, else a `reference` directory beside
+this repository; `nb3` regenerates only the Neighbor3D tables.
 
 Three reference sources are used, and nothing else:
   * tiralib's own C++ CPU functions, compiled unmodified by oracle/build_ref.sh
@@ -227,10 +230,37 @@ def main(ref_root):
         vals.append(met.simf(G, B.reshape(H, W, 2, 2).astype(np.float32)))
     fx["sweep_simf"] = np.array(vals, np.float64)
     np.savez_compressed(os.path.join(HERE, "reconstruct_reference.npz"), **fx)
+    make_neighbors3d(ref_root)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))
 
 
+def make_neighbors3d(ref_root):
+    """tira::Neighbor3D tables from the reference's cpu::build_neighbors3d
+    (tensorvote.h:1411), for the library's host-side table builder."""
+    O.build(ref_root)
+    assert O.ref_available(), "reference CPU library did not build"
+    fx = {}
+    for (w, s1, s2) in [(5, 1.5, 0.0), (7, 2.0, 0.5), (9, 0.0, 1.0)]:
+        fx[f"nb3_w{w}_{s1}_{s2}"] = O.build_neighbors3d_ref(w, s1, s2)
+    np.savez_compressed(os.path.join(HERE, "nb3_cpp_reference.npz"), **fx)
+
+
+def reference_root(argv):
+    """The tiralib checkout: the first argument, else $TIRALIB_REFERENCE, else
+    a `reference` directory beside this repository."""
+    if len(argv) > 1:
+        return argv[1]
+    env = os.environ.get("TIRALIB_REFERENCE")
+    if env:
+        return env
+    return os.path.join(os.path.dirname(os.path.dirname(os.path.dirname(HERE))), "reference")
+
+
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = reference_root(sys.argv[:2])
+    if len(sys.argv) > 2 and sys.argv[2] == "nb3":
+        make_neighbors3d(root)
+    else:
+        main(root)

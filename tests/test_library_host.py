@@ -49,6 +49,29 @@ def test_neighbors2d_table_matches_reference(tv, golden):
         np.testing.assert_allclose(nb[f], ref[f], rtol=0, atol=2e-6)
 
 
+def test_neighbors3d_table_matches_reference(tv, golden):
+    """tvgb_build_neighbors3d against the reference's cpu::build_neighbors3d
+    (tensorvote.h:1411), bit for bit, including sigma = 0 rows."""
+    g = golden("nb3_cpp_reference.npz")
+    for key in g.files:
+        w, s1, s2 = key.split("_")[1:]
+        nb = tv.build_neighbors3d(int(w[1:]), float(s1), float(s2))
+        ref = g[key]
+        assert nb.dtype.itemsize == 32 and nb.size == ref.size
+        for f in nb.dtype.names:
+            np.testing.assert_array_equal(nb[f], ref[f], err_msg=f"{key}.{f}")
+
+
+def test_tensorvote3_rejects_a_negative_device(tv):
+    """The reference's negative device index selects its CPU path
+    (eigen.h:897); this library has none and says so instead of running on
+    whatever device is current."""
+    T = np.zeros((2, 2, 2, 9), np.float32)
+    out = np.zeros_like(T)
+    with pytest.raises(tv.TvgbError, match="CPU path"):
+        tv.tensorvote3(T, out, 2, 2, 2, 1.0, 0.0, 3, 1, device=-1)
+
+
 def test_sticknorm3_matches_oracle(tv):
     from oracle import oracle as O
     for args in [(4.0, 0.0, 1), (2.0, 1.0, 3), (6.0, 0.5, 2)]:

@@ -28,3 +28,30 @@ def test_shim_header_compiles_and_links(tmp_path):
         pytest.skip("nvcc not available")
     exe = build_shim_check(str(tmp_path))
     assert os.path.exists(exe)
+
+
+def test_shim_host_calls_in_the_reference_form(tmp_path, golden):
+    """build_neighbors2d / build_neighbors3d called as the reference declares
+    them (std::vector results, tensorvote.h:1222, 1411) give the reference's
+    tables, and an eigen launcher asked for device -1 (the reference's CPU
+    path, eigen.h:897) reports an error and returns nullptr."""
+    import numpy as np
+    from tiralib_gb300.api import NB2_DTYPE, NB3_DTYPE
+    if shutil.which("nvcc") is None and not os.path.exists("/usr/local/cuda/bin/nvcc"):
+        pytest.skip("nvcc not available")
+    exe = build_shim_check(str(tmp_path))
+    out = os.path.join(str(tmp_path), "host.bin")
+    r = subprocess.run([exe, "--host", out], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "CPU path" in r.stdout            # the printed error names the missing CPU path
+    raw = open(out, "rb").read()
+    n2, n3, null_ev = np.frombuffer(raw[:12], np.int32)
+    assert (n2, n3, null_ev) == (49, 343, 1)
+    nb2 = np.frombuffer(raw[12:12 + 48 * n2], NB2_DTYPE)
+    nb3 = np.frombuffer(raw[12 + 48 * n2:], NB3_DTYPE)
+    ref2 = golden("tv2_cpp_reference.npz")["nb_w7"]
+    for f in NB2_DTYPE.names:
+        np.testing.assert_allclose(nb2[f], ref2[f], rtol=0, atol=2e-6)
+    ref3 = golden("nb3_cpp_reference.npz")["nb3_w7_2.0_0.5"]
+    for f in NB3_DTYPE.names:
+        np.testing.assert_array_equal(nb3[f], ref3[f])

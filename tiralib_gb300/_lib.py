@@ -64,6 +64,7 @@ SIGNATURES = {
     "tvgb_tensorvote": (_I, [_P, _P, _F, _F, _I, _U, _U, _U, _I, _I, _U, _I, _P]),
     "tvgb_tensorvote_prebuilt": (_I, [_P, _P, _P, _I, _F, _F, _I, _U, _U, _U, _I, _I, _U, _P]),
     "tvgb_build_neighbors2d": (_I, [_I, _F, _F, _U, _U, _I, _I, _P, ctypes.POINTER(ctypes.c_int)]),
+    "tvgb_build_neighbors3d": (_I, [_I, _F, _F, _P, ctypes.POINTER(ctypes.c_int)]),
     "tvgb_vote3": (_I, [_P, _I, _U, _U, _U, ctypes.POINTER(Vote3Params), _P, _I, _P, _P, _I, _P]),
     "tvgb_vote3_noalloc": (_I, [_P, _I, _U, _U, _U, ctypes.POINTER(Vote3Params), _P, _I, _P, _P, _I, _P]),
     "tvgb_pipeline3": (_I, [_P, _U, _U, _U, _F, _I, ctypes.POINTER(Vote3Params), _P, _I, _P, _P, _I, _P, _P]),

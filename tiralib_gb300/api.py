@@ -10,6 +10,7 @@ and meaning follow the reference:
   tensorvote             tira::cuda::tensorvote       tensorvote.h:2201
   tensorvote_prebuilt    tira::cuda::tensorvote_prebuilt  tensorvote.h:2237
   build_neighbors2d      tira::cpu::build_neighbors2d tensorvote.h:1223
+  build_neighbors3d      tira::cpu::build_neighbors3d tensorvote.h:1411
   evals3_symmetric       tira::cuda::evals3_symmetric eigen.h:896
   evecs3spherical_symmetric                           eigen.h:945
   evals2_symmetric / evecs2polar_symmetric            eigen.h:769 / :828
@@ -44,6 +45,12 @@ NB2_DTYPE = np.dtype([
     ("Ra", np.float32), ("Rb", np.float32), ("Rc", np.float32),
     ("Va", np.float32), ("Vb", np.float32), ("Vc", np.float32),
 ])  # tira::Neighbor2D, 48 bytes (tensorvote.h:776)
+
+NB3_DTYPE = np.dtype([
+    ("du", np.int32), ("dv", np.int32), ("dw", np.int32),
+    ("d", np.float32, (3,)),
+    ("c1", np.float32), ("c2", np.float32),
+])  # tira::Neighbor3D, 32 bytes (tensorvote.h:1147)
 
 
 # ----------------------------------------------------------------- array helpers
@@ -273,6 +280,15 @@ def build_neighbors2d(w, sigma1, sigma2, power, samples, stick=True, plate=True)
     return out[: cnt.value]
 
 
+def build_neighbors3d(w, sigma1, sigma2=0.0):
+    """tira::cpu::build_neighbors3d (tensorvote.h:1411; sigma = (sigma1,
+    sigma2)) -> NB3_DTYPE array of w**3 records, dw outermost."""
+    out = np.zeros(max(w, 0) ** 3, NB3_DTYPE)
+    cnt = ctypes.c_int(0)
+    call("tvgb_build_neighbors3d", int(w), sigma1, sigma2, ctypes.c_void_p(out.ctypes.data), ctypes.byref(cnt))
+    return out[: cnt.value]
+
+
 def sticknorm3(sigma1, sigma2, power):
     return _lib.lib().tvgb_sticknorm3(sigma1, sigma2, power)
 
@@ -354,6 +370,7 @@ def memory_stats(reset_peak=False):
 __all__ = [
     "TvgbError", "NB2_DTYPE", "evals3_symmetric", "evecs3spherical_symmetric", "evals2_symmetric",
     "evecs2polar_symmetric", "eig3", "gaussian_filter3d", "gaussian_convolve2", "structure_tensor3",
-    "structure_tensor2", "tensorvote3", "tensorvote", "tensorvote_prebuilt", "build_neighbors2d", "sticknorm3",
+    "structure_tensor2", "tensorvote3", "tensorvote", "tensorvote_prebuilt", "build_neighbors2d", "build_neighbors3d",
+    "NB3_DTYPE", "sticknorm3",
     "make_params", "vote3", "pipeline3", "launch_count", "memory_stats",
 ]

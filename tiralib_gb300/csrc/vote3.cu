@@ -372,6 +372,19 @@ __device__ __forceinline__ void write_receiver(const FastArgs& a, size_t idx, si
     }
 }
 
+// No term votes: every receiver's voted tensor is zero.  Writes the zero
+// tensor and, where asked for, its eigendecomposition through the same
+// epilogue as the vote kernels, so the outputs match a vote whose terms all
+// contribute nothing.
+__global__ void __launch_bounds__(256) k_vote3_none(FastArgs a) {
+    const size_t n = size_t(a.s0) * a.s1 * a.s2, plane = size_t(a.s1) * a.s2;
+    const size_t i1 = size_t(a.zr1) * plane;      // receivers of planes [zr0, zr1)
+    const float zero6[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    for (size_t i = size_t(a.zr0) * plane + size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < i1;
+         i += size_t(gridDim.x) * blockDim.x)
+        write_receiver(a, i, n, zero6);
+}
+
 template <int R, bool STICK, bool PLATE, bool BALL>
 __global__ void __launch_bounds__(VX * VY, TVGB_FAST_MINB) k_vote3_fast(FastArgs a) {
     extern __shared__ __align__(16) float4 smem[];
@@ -1018,9 +1031,23 @@ static size_t pk_smem(int hw, int rows, bool S, bool P, bool B) {
     return fast_smem(hw, rows, S, P, B) + 2 * ne * (B ? 4 : 3) * 16;
 }
 
+static int launch_none(const FastArgs& a, cudaStream_t st) {
+    const size_t n = size_t(a.zr1 - a.zr0) * a.s1 * a.s2;
+    if (n == 0) return TVGB_OK;
+    const size_t blocks = std::min<size_t>((n + 255) / 256, 152 * 8);
+    {
+        KernelTimer kt_("k_vote3_none", st);
+        k_vote3_none<<<unsigned(blocks), 256, 0, st>>>(a);
+        kt_.stop();
+    }
+    TVGB_LAUNCHED();
+    return TVGB_OK;
+}
+
 static int launch_fast(FastArgs a, bool S, bool P, bool B, cudaStream_t st) {
     if (a.zr1 <= a.zr0) { a.zr0 = 0; a.zr1 = a.s0; }   // every receiver plane
     if (a.zr1 <= a.zr0) return TVGB_OK;
+    if (!S && !P && !B) return launch_none(a, st);
     // rows per stage: the largest count that keeps TVGB_FAST_MINB CTAs per SM
     const int w = 2 * a.hw + 1;
     const size_t budget = (TVGB_FAST_MINB >= 3 ? 72 : 100) * 1024;
@@ -1242,6 +1269,41 @@ extern "C" {
 
 double tvgb_sticknorm3(float sigma1, float sigma2, unsigned power) { return sticknorm3_f(sigma1, sigma2, power); }
 
+// Host table of tira::Neighbor3D records (tensorvote.h:1147, built by
+// cpu::build_neighbors3d :1411): 32 bytes each, int32 du, dv, dw, float32
+// d.x, d.y, d.z, c1, c2, with du on the fast axis and dw on the slow one, in
+// the reference's loop order (dw outermost) and float steps.  The vote
+// kernels here index a radial table instead; this exists for callers that
+// inspect or reuse the reference's table.
+int tvgb_build_neighbors3d(int w, float sigma1, float sigma2, void* out, int* count) {
+    TVGB_CHECK_ARG(count, "tvgb_build_neighbors3d: count is NULL");
+    TVGB_CHECK_ARG(w >= 0, "tvgb_build_neighbors3d: w must be >= 0");
+    TVGB_CHECK_ARG(w <= 1025, "tvgb_build_neighbors3d: w = %d too large", w);
+    struct Nb3 { int du, dv, dw; float dx, dy, dz, c1, c2; };
+    static_assert(sizeof(Nb3) == 32, "Neighbor3D must be 32 bytes");
+    const int hw = w / 2;
+    const float inv1 = sigma1 > 0 ? 1.0f / (sigma1 * sigma1) : 0.0f, inv2 = sigma2 > 0 ? 1.0f / (sigma2 * sigma2) : 0.0f;
+    Nb3* o = static_cast<Nb3*>(out);
+    int k = 0;
+    for (int dw = -hw; dw <= hw; dw++)
+        for (int dv = -hw; dv <= hw; dv++)
+            for (int du = -hw; du <= hw; du++, k++) {
+                if (!o) continue;
+                Nb3 e{};
+                e.du = du; e.dv = dv; e.dw = dw;
+                const float l2 = float(du * du + dv * dv + dw * dw);
+                if (l2 != 0.0f) {
+                    const float len = std::sqrt(l2);
+                    e.dx = float(du) / len; e.dy = float(dv) / len; e.dz = float(dw) / len;
+                }
+                e.c1 = sigma1 == 0.0f ? (l2 > 1e-12f ? 0.0f : 1.0f) : std::exp(-l2 * inv1);
+                e.c2 = sigma2 == 0.0f ? (l2 > 1e-12f ? 0.0f : 1.0f) : std::exp(-l2 * inv2);
+                o[k] = e;
+            }
+    *count = k;
+    return TVGB_OK;
+}
+
 static int check_params(const tvgb_vote3_params* p, const char* fn) {
     TVGB_CHECK_ARG(p, "%s: params is NULL", fn);
     TVGB_CHECK_ARG(p->sigma1 >= 0.0f && p->sigma2 >= 0.0f, "%s: sigmas must be >= 0", fn);
@@ -1294,7 +1356,11 @@ int tvgb_tensorvote3(const float* input_field, float* output_field, unsigned s0,
                      int is_atv, void* stream) {
     TVGB_CHECK_ARG(input_field && output_field, "tvgb_tensorvote3: NULL field pointer");
     TVGB_CHECK_ARG(w >= 1 && (w % 2) == 1, "tvgb_tensorvote3: window w must be odd and >= 1 (got %u)", w);
-    if (device >= 0) TVGB_CUDA(cudaSetDevice(device));
+    // the reference runs on device `device` (tensorvote.h:2820); a negative
+    // index selects its CPU eigen path (eigen.h:897), which this library has not
+    TVGB_CHECK_ARG(device >= 0, "tvgb_tensorvote3: device %d: negative indices select the reference's CPU path, "
+                   "which this GPU library does not provide", device);
+    TVGB_CUDA(cudaSetDevice(device));
     tvgb_vote3_params p{};
     p.sigma1 = sigma; p.sigma2 = sigma2; p.w = w; p.power = power; p.samples = samples;
     p.stick = stick; p.plate = plate; p.ball = 0; p.is_atv = is_atv; p.parity = 1;
@@ -1399,10 +1465,7 @@ extern "C" int tvgb_vote3_noalloc(const float* in, int in_layout, unsigned s0, u
     fa.out = out; fa.out_layout = out_layout; fa.evals = evals3;
     fa.evecs = evec_format ? evecs : nullptr; fa.evec_fmt = evec_format;
     fa.precise_eig = p->parity ? 0 : 1;
-    if (!S && !P && !B) {
-        if (out) TVGB_CUDA(cudaMemsetAsync(out, 0, n * (out_layout == TVGB_LAYOUT_MAT3 ? 36 : 24), st));
-        return TVGB_OK;
-    }
+    // with no term voting, launch_fast writes the zero tensor and its eigendecomposition
     return launch_fast(fa, S, P, B, st);
 }
 
