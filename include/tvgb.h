@@ -292,6 +292,17 @@ int tvgb_surrogate_eval(const float* params, const float* X, size_t n, float* Y,
  * surrogate vote).  Returns TVGB_ERR_CUDA if a tensor-core wait timed out. */
 int tvgb_surrogate_eval_tc(const float* params, const float* X, size_t n, float* Y, int gelu_mode, void* stream);
 
+/* tvgb_surrogate_eval_tc with the bound on each layer's wait for its MMAs
+ * made explicit (no reference counterpart): wait_limit < 0 is the default
+ * (2^24 mbarrier polls), 0 <= wait_limit <= 2^24 that many polls.  A wait
+ * that runs out makes every thread of the CTA stop at its next layer; the
+ * MMAs still in flight are then waited for with the full default bound
+ * before the tensor memory is released, and the call returns TVGB_ERR_CUDA
+ * with the device context intact.  wait_limit = 0 gives up at once: it
+ * exists to test that path. */
+int tvgb_surrogate_eval_tc_limit(const float* params, const float* X, size_t n, float* Y, int gelu_mode,
+                                 long long wait_limit, void* stream);
+
 /* tvgb_vote3 (TK, power 1, sigma2 = 0) with the plate (and ball) vote by
  * plate_mode: 0 the network (judged per CTA of 32 x 4 receivers: if any of
  * its first 32 receivers' plate differs from the exact plate by more than

@@ -40,6 +40,56 @@ def tensor_rel(a, ref):
     return np.sqrt((WGT * (a - ref) ** 2).sum(1) / np.maximum((WGT * ref ** 2).sum(1), 1e-300))
 
 
+EPS32 = 2.0 ** -24
+SAMPLE = 8      # receiver block side of the CPU samples
+
+
+def six_to_mat(t6):
+    t = np.asarray(t6, np.float64)
+    return np.stack([t[:, 0], t[:, 1], t[:, 2], t[:, 1], t[:, 3], t[:, 4], t[:, 2], t[:, 4], t[:, 5]],
+                    axis=1).reshape(-1, 3, 3)
+
+
+def check_eigenvectors(gvec, rvec, g6, r6, rev, label, c_solver=64.0):
+    """Eigenvectors up to sign against a reference decomposition, bounded by
+    their conditioning.  For eigenvector k with eigenvalue gap g_k = min over
+    j != k of |lambda_k - lambda_j| (reference eigenvalues), a perturbation E
+    of the tensor turns it by at most ~||E|| / g_k (Davis-Kahan), so each
+    angle must satisfy
+
+        angle_k <= (2 ||T_gpu - T_ref||_F + c_solver eps32 ||T_ref||_F) / g_k :
+
+    the first term the two voted tensors' own difference, the second the
+    FP32 closed-form solver's rounding.  Where that bound is below 1e-4 rad
+    (well-separated eigenvalues: on these fields most receivers' e2), the
+    the benchmark spec's 1e-4 bar applies directly, and at least a quarter of the
+    sample's e2 vectors must be in that class so the check is not vacuous.
+    Angles are atan2(|u x v|, |u . v|)
+    of the normalised vectors (arccos of a dot product would turn the ~1e-7
+    norm error of an FP32 vector into a spurious 3e-4 rad)."""
+    g = np.asarray(gvec, np.float64)
+    g = g / np.linalg.norm(g, axis=2, keepdims=True)
+    r = np.asarray(rvec, np.float64)
+    r = r / np.linalg.norm(r, axis=2, keepdims=True)
+    ang = np.arctan2(np.linalg.norm(np.cross(g, r), axis=2), np.abs((g * r).sum(2)))     # (n, 3)
+    Tn = np.linalg.norm(six_to_mat(r6).reshape(-1, 9), axis=1)
+    dT = np.linalg.norm((six_to_mat(g6) - six_to_mat(r6)).reshape(-1, 9), axis=1)
+    lam = np.asarray(rev, np.float64)
+    gaps = np.stack([np.minimum(np.abs(lam[:, 0] - lam[:, 1]), np.abs(lam[:, 0] - lam[:, 2])),
+                     np.minimum(np.abs(lam[:, 1] - lam[:, 0]), np.abs(lam[:, 1] - lam[:, 2])),
+                     np.minimum(np.abs(lam[:, 2] - lam[:, 0]), np.abs(lam[:, 2] - lam[:, 1]))], axis=1)
+    bound = (2.0 * dT + c_solver * EPS32 * Tn)[:, None] / np.maximum(gaps, 1e-300)
+    ratio = ang / bound
+    worst = np.unravel_index(int(np.argmax(ratio)), ratio.shape)
+    assert ratio.max() <= 1.0, (f"{label}: eigenvector e{worst[1]} of receiver {worst[0]} turned {ang[worst]:.3e} rad, "
+                                f"bound {bound[worst]:.3e} (gap/||T|| {gaps[worst] / Tn[worst[0]]:.3e}, "
+                                f"||dT||/||T|| {dT[worst[0]] / Tn[worst[0]]:.3e})")
+    sep = bound < 1e-4
+    assert sep[:, 2].mean() >= 0.25, f"{label}: only {sep[:, 2].mean():.2f} of the e2 vectors are well separated"
+    assert ang[sep].max() < 1e-4, f"{label}: well-separated eigenvector turned {ang[sep].max():.3e} rad"
+    return float(ang[:, 2].max()), float(ang[:, 0].max())
+
+
 def run3(tv, vol, cfg, parity):
     return tv.pipeline3(vol, cfg["sigma_st"], cfg["sigma"], w=cfg["w"], samples=cfg["samples"], ball=cfg["ball"],
                         parity=parity, out_layout="planes", evals=True, evecs="cartesian")
@@ -75,8 +125,9 @@ def check_field_properties(torch, out, ev, vec):
 @pytest.mark.parametrize("name", ["c2", "c4"])
 def test_tube_field_at_full_size(torch_dev, name):
     """C2 (256^3) and C4 (384^3), sigma 4, w 25: the whole field's properties,
-    exact scaling, and a 4^3 receiver sample against the reference's CPU
-    algorithm."""
+    exact scaling, and an 8^3 receiver sample against the reference's CPU
+    algorithm (voted tensors, eigenvalues and eigenvectors, parity mode) and
+    against the FP64 oracle (precise mode)."""
     torch, dev = torch_dev
     import tiralib_gb300 as tv
     cfg = dict(bench.CONFIGS3[name])
@@ -86,17 +137,27 @@ def test_tube_field_at_full_size(torch_dev, name):
     torch.cuda.synchronize()
     # the reference's CPU algorithm (parity mode) on a sample of receivers
     detail = {}
-    bench.cpu_reference_sample(vol_d.cpu().numpy(), cfg, block=4, seed=7, threads=THREADS, detail=detail)
+    bench.cpu_reference_sample(vol_d.cpu().numpy(), cfg, block=SAMPLE, seed=7, threads=THREADS, detail=detail)
     g6, gev, gvec = at_block(detail, out, ev, vec)
     c6 = detail["voted"].reshape(-1, 9)[:, [0, 1, 2, 4, 5, 8]].astype(np.float64)
     assert tensor_rel(g6, c6).max() < 1e-4
     cev = detail["evals"].astype(np.float64)
     assert (np.abs(gev - cev).max(1) / np.abs(cev).max(1)).max() < 1e-4
+    # eigenvectors (eigen.h's evec3_symmetric on both sides, eigen.h:452) up to sign
+    check_eigenvectors(gvec, detail["evecs"].reshape(-1, 3, 3), g6, c6, cev, f"{name} parity vs reference CPU")
     del out, ev, vec
     # precise mode: the whole field's properties, and exact power-of-two scaling of the whole pipeline
     p1 = run3(tv, vol_d, cfg, parity=False)
     torch.cuda.synchronize()
     check_field_properties(torch, *p1)
+    # the sample against the FP64 oracle: FP64 voter eigenvectors, FP64 vote, FP64 Jacobi eigenpairs
+    g6p, gevp, gvecp = at_block(detail, *p1)
+    f64 = O.tensorvote3_f64(detail["field"], cfg["sigma"], 0.0, cfg["w"], 1, ball=cfg["ball"],
+                            receivers=detail["receivers"], threads=THREADS).reshape(-1, 6)[detail["receivers"]]
+    assert tensor_rel(g6p, f64).max() < 1e-5
+    fev, fvec = O.eig3_f64(f64)
+    assert (np.abs(gevp - fev).max(1) / np.abs(fev).max(1)).max() < 1e-5
+    check_eigenvectors(gvecp, fvec, g6p, f64, fev, f"{name} precise vs FP64")
     p2 = run3(tv, 2.0 * vol_d, cfg, parity=False)
     torch.cuda.synchronize()
     assert torch.equal(p2[0], 4.0 * p1[0])
@@ -106,8 +167,9 @@ def test_tube_field_at_full_size(torch_dev, name):
 
 def test_capacity_field_with_ball_at_full_size(torch_dev):
     """C5 (512^3 tubes and sheets, sigma 6, w 37, stick + plate + ball) in
-    precise mode: the whole field's properties and a 4^3 receiver sample
-    against the FP64 oracle (the reference has no TK ball term)."""
+    precise mode: the whole field's properties and an 8^3 receiver sample
+    against the FP64 oracle, eigenvectors included (the reference has no TK
+    ball term)."""
     torch, dev = torch_dev
     import tiralib_gb300 as tv
     cfg = dict(bench.CONFIGS3["c5"])
@@ -116,13 +178,14 @@ def test_capacity_field_with_ball_at_full_size(torch_dev):
     torch.cuda.synchronize()
     check_field_properties(torch, out, ev, vec)
     detail = {}
-    bench.cpu_reference_sample(vol.cpu().numpy(), cfg, block=4, seed=7, threads=THREADS, detail=detail)
-    g6, gev, _ = at_block(detail, out, ev, vec)
+    bench.cpu_reference_sample(vol.cpu().numpy(), cfg, block=SAMPLE, seed=7, threads=THREADS, detail=detail)
+    g6, gev, gvec = at_block(detail, out, ev, vec)
     f64 = O.tensorvote3_f64(detail["field"], cfg["sigma"], 0.0, cfg["w"], 1, ball=True,
                             receivers=detail["receivers"], threads=THREADS).reshape(-1, 6)[detail["receivers"]]
     assert tensor_rel(g6, f64).max() < 1e-5
-    fev, _ = O.eig3_f64(f64)
+    fev, fvec = O.eig3_f64(f64)
     assert (np.abs(gev - fev).max(1) / np.abs(fev).max(1)).max() < 1e-5
+    check_eigenvectors(gvec, fvec, g6, f64, fev, "c5 precise vs FP64")
 
 
 def test_eigen_batch_at_full_size(torch_dev):

@@ -89,6 +89,24 @@ def test_tcgen05_inference_ragged_sizes(S):
         assert np.median(err) <= 2e-3 * scale and err.max() <= 3e-2 * scale, n
 
 
+def test_tcgen05_wait_that_runs_out_returns_an_error(S):
+    """Each layer of the tensor-core network waits for its MMAs on an
+    mbarrier for a bounded number of polls.  With a bound of zero polls every
+    wait runs out at once: the kernel stops at the next layer, waits for the
+    MMAs still in flight with the full bound, releases its tensor memory and
+    reports the timeout, so the call raises and the context stays usable.
+    The next call with the default bound gives the same outputs, bit for bit,
+    as the call before the failure."""
+    from tiralib_gb300 import TvgbError
+    p = S.init_params(3)
+    X, _ = S.samples(20_000, seed=4)
+    Y0 = S.evaluate(p, X)
+    with pytest.raises(TvgbError, match="timed out"):
+        S.evaluate(p, X, wait_limit=0)
+    Y1 = S.evaluate(p, X)
+    np.testing.assert_array_equal(Y0, Y1)
+
+
 def test_training_reduces_the_loss(S, trained):
     p, hist = trained
     assert np.all(np.isfinite(hist))

@@ -222,3 +222,22 @@ def test_vote3_host_outputs_in_slabs_equal_device_outputs():
     np.testing.assert_array_equal(o_h, o_d.cpu().numpy())
     np.testing.assert_array_equal(ev_h, ev_d.cpu().numpy())
     np.testing.assert_array_equal(vec_h, vec_d.cpu().numpy())
+
+
+@pytest.mark.parametrize("parity", [True, False])
+def test_vote3_with_no_terms_gives_the_zero_tensors_eigendecomposition(parity):
+    """stick = plate = ball = 0 with eigen outputs requested: the voted field
+    is zero and every receiver gets the zero tensor's eigendecomposition (the
+    same the eigensolver gives it: eigenvalues 0, the identity frame), not
+    whatever the arrays held before."""
+    import torch
+    import tiralib_gb300 as tv
+    dev = torch.device("cuda:0")
+    T = torch.from_numpy(spd_field((5, 6, 7), 4)).to(dev)
+    out, ev, vec = tv.vote3(T, 1.5, w=5, stick=False, plate=False, ball=False, parity=parity, out_layout="sym6",
+                            evals=True, evecs="cartesian")
+    torch.cuda.synchronize()
+    assert float(out.abs().max()) == 0.0
+    assert float(ev.abs().max()) == 0.0
+    ref = O.evecs3cart(np.zeros((1, 9), np.float32), np.zeros((1, 3), np.float32))[0]
+    np.testing.assert_array_equal(vec.cpu().numpy().reshape(-1, 3, 3), np.broadcast_to(ref, (5 * 6 * 7, 3, 3)))

@@ -84,3 +84,27 @@ def test_noalloc_vote_refuses_oversize_and_host_arrays():
                               ctypes.c_void_p(out_h.ctypes.data), 6, None, None, 0, None)
     assert rc == 1
     assert "device memory" in L.tvgb_last_error().decode()
+
+
+def test_noalloc_vote_with_no_terms_writes_eigen_outputs():
+    """With no term voting, the allocation-free entry point still fills the
+    requested eigenvalue array (the zero tensor's eigenvalues), as the
+    allocating entry point does."""
+    import torch
+    import tiralib_gb300 as tv
+    from tiralib_gb300 import _lib
+    L = _lib.lib()
+    dev = torch.device("cuda:0")
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    shape = (6, 7, 8)
+    t_dev = torch.from_numpy(spd_field(shape, 5)).to(dev)
+    params = tv.make_params(2.0, 0.0, w=5, stick=False, plate=False, ball=False)
+    out = torch.full(shape + (6,), float("nan"), device=dev)
+    ev = torch.full(shape + (3,), float("nan"), device=dev)
+    rc = _call(L, t_dev, shape, params, out, ev, stream)
+    torch.cuda.synchronize()
+    assert rc == 0, L.tvgb_last_error().decode()
+    ref_out, ref_ev, _ = tv.vote3(t_dev, 2.0, w=5, stick=False, plate=False, out_layout="sym6", evals=True)
+    torch.cuda.synchronize()
+    assert torch.equal(out, ref_out) and torch.equal(ev, ref_ev)
+    assert float(ev.abs().max()) == 0.0

@@ -42,6 +42,7 @@ SIGNATURES = {
     "tvgb_surrogate_train": (_I, [_P, _P, _P, _SZ, _I, _I, _F, _P, _P]),
     "tvgb_surrogate_eval": (_I, [_P, _P, _SZ, _P, _P]),
     "tvgb_surrogate_eval_tc": (_I, [_P, _P, _SZ, _P, _I, _P]),
+    "tvgb_surrogate_eval_tc_limit": (_I, [_P, _P, _SZ, _P, _I, ctypes.c_longlong, _P]),
     "tvgb_vote3_surrogate": (_I, [_P, _I, _U, _U, _U, ctypes.POINTER(Vote3Params), _P, _I, _F, _P, _I, _P, _P, _I,
                                   _P, _P]),
     "tvgb_stick_saliency2": (_I, [_P, _SZ, _P, _P]),

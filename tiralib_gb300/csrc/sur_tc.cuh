@@ -103,14 +103,18 @@ struct SurTc {
     uint32_t img;        // shared-memory address of the weight image
     uint64_t* bar;       // MMA completion barrier
     uint32_t phase;      // parity of the next completion
+    uint32_t wait_limit; // polls of each layer's MMA barrier before the thread gives up
     int failed;          // this thread's wait gave up
 };
 
 // Setup by all 128 threads: weight image global -> shared memory, barrier,
 // TMEM allocation (warp 0), the constant block.  tmem_slot and bar are
-// __shared__ variables of the caller.  Ends with a CTA barrier.
+// __shared__ variables of the caller.  wait_limit bounds each layer's wait
+// for its MMAs (polls; 0 gives up at once, which only tests the error path).
+// Ends with a CTA barrier.
 __device__ __forceinline__ void sur_tc_setup(SurTc& s, const uint4* __restrict__ img_g, uint4* img_s,
-                                             uint32_t* tmem_slot, uint64_t* bar) {
+                                             uint32_t* tmem_slot, uint64_t* bar,
+                                             uint32_t wait_limit = TC_WAIT_LIMIT) {
     const int tid = threadIdx.x;
     for (int i = tid; i < TC_IMG_BYTES / 16; i += blockDim.x) img_s[i] = img_g[i];
     if (tid == 0) tc::mbar_init(bar, 1);
@@ -126,6 +130,7 @@ __device__ __forceinline__ void sur_tc_setup(SurTc& s, const uint4* __restrict__
     s.img = tc::smem_u32(img_s);
     s.bar = bar;
     s.phase = 0;
+    s.wait_limit = wait_limit;
     s.failed = 0;
     const uint32_t one[8] = {0x3F803F80u, 0, 0, 0, 0, 0, 0, 0};   // bf16 (1, 1)
     tc::tmem_st8(s.tmem + tc_lane_base() + TC_ONE, one);
@@ -154,15 +159,17 @@ __device__ __forceinline__ bool sur_tc_layer(SurTc& s) {
         }
         tc::mma_commit(s.bar);
     }
-    if (tc::mbar_wait(s.bar, s.phase, TC_WAIT_LIMIT)) s.phase ^= 1u;
+    if (tc::mbar_wait(s.bar, s.phase, s.wait_limit)) s.phase ^= 1u;
     else s.failed = 1;            // the phase stays: teardown waits for it
     tc::fence_after_sync();
     return true;
 }
 
-// GELU of this thread's row of D into its row of A
+// GELU of this thread's row of D into its row of A.  A thread whose wait
+// gave up leaves tensor memory alone: its MMAs may still be in flight.
 template <int GM>
 __device__ __forceinline__ void sur_tc_hidden(const SurTc& s) {
+    if (s.failed) return;
     const uint32_t t = s.tmem + tc_lane_base();
     uint32_t act[32];
 #pragma unroll
@@ -197,8 +204,8 @@ __device__ __forceinline__ bool sur_tc_layers(SurTc& s) {
 template <int GM>
 __device__ __forceinline__ bool sur_tc_forward(SurTc& s, const uint32_t (&in)[8], float (&out)[8]) {
     const uint32_t t = s.tmem + tc_lane_base();
-    tc::tmem_st8(t + TC_A, in);
-    if (!sur_tc_layers<GM>(s)) return false;
+    if (!s.failed) tc::tmem_st8(t + TC_A, in);
+    if (!sur_tc_layers<GM>(s) || s.failed) return false;
     uint32_t r[16];
     tc::tmem_ld16(t + TC_D, r);
 #pragma unroll
@@ -208,11 +215,14 @@ __device__ __forceinline__ bool sur_tc_forward(SurTc& s, const uint32_t (&in)[8]
 
 // Teardown by all threads: TMEM freed by warp 0.  Returns false if a wait
 // gave up anywhere in the CTA; then the MMAs still in flight are waited for
-// (bounded) before the columns are released.
+// before the columns are released, always with the full TC_WAIT_LIMIT
+// whatever the layers' limit was.  Only thread 0's own phase can still be
+// pending: once any wait gives up no further MMA is issued, and if thread 0's
+// last wait succeeded, the MMAs it issued have completed.
 __device__ __forceinline__ bool sur_tc_teardown(SurTc& s) {
     tc::fence_before_sync();
     const int bad = __syncthreads_or(s.failed);
-    if (bad && threadIdx.x == 0) tc::mbar_wait(s.bar, s.phase, TC_WAIT_LIMIT);
+    if (bad && threadIdx.x == 0 && s.failed) tc::mbar_wait(s.bar, s.phase, TC_WAIT_LIMIT);
     __syncthreads();
     tc::fence_after_sync();
     if (threadIdx.x < 32) tc::tmem_dealloc(s.tmem, TC_COLS);

@@ -375,12 +375,13 @@ __global__ void __launch_bounds__(128) k_sur_eval(const uint2* __restrict__ frag
 // The network on tcgen05: one 128-sample tile per CTA iteration (sur_tc.cuh).
 template <int GM>
 __global__ void __launch_bounds__(128) k_sur_eval_tc(const uint4* __restrict__ img_g, const float* __restrict__ X,
-                                                     size_t n, float* __restrict__ Y, int* __restrict__ err) {
+                                                     size_t n, float* __restrict__ Y, int* __restrict__ err,
+                                                     uint32_t wait_limit) {
     extern __shared__ __align__(128) uint4 img_s[];
     __shared__ uint32_t tmem_slot;
     __shared__ __align__(8) uint64_t bar;
     SurTc s;
-    sur_tc_setup(s, img_g, img_s, &tmem_slot, &bar);
+    sur_tc_setup(s, img_g, img_s, &tmem_slot, &bar, wait_limit);
     const size_t ntiles = (n + 127) / 128;
     for (size_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const size_t row = tile * 128 + threadIdx.x;
@@ -418,7 +419,7 @@ int sur_upload_tc(const float* params_host_or_dev, void* img_dev, cudaStream_t s
 }
 
 int sur_eval_tc_device(const void* img, const float* X, size_t n, float* Y, int gelu_mode, int* err,
-                       cudaStream_t st) {
+                       cudaStream_t st, uint32_t wait_limit) {
     if (n == 0) return TVGB_OK;
     const size_t tiles = (n + 127) / 128;
     const unsigned grid = unsigned(tiles < 152 * 4 ? tiles : 152 * 4);
@@ -426,7 +427,7 @@ int sur_eval_tc_device(const void* img, const float* X, size_t n, float* Y, int 
     const void* fn = gelu_mode == 0 ? (const void*)k_sur_eval_tc<0> : (const void*)k_sur_eval_tc<1>;
     TVGB_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     const uint4* img4 = static_cast<const uint4*>(img);
-    void* args[] = {&img4, &X, &n, &Y, &err};
+    void* args[] = {&img4, &X, &n, &Y, &err, &wait_limit};
     {
         KernelTimer kt_("k_sur_eval_tc", st);
         TVGB_CUDA(cudaLaunchKernel(fn, dim3(grid), dim3(128), args, smem, st));
@@ -599,8 +600,16 @@ int tvgb_surrogate_eval(const float* params, const float* X, size_t n, float* Y,
 }
 
 int tvgb_surrogate_eval_tc(const float* params, const float* X, size_t n, float* Y, int gelu_mode, void* stream) {
+    return tvgb_surrogate_eval_tc_limit(params, X, n, Y, gelu_mode, -1, stream);
+}
+
+int tvgb_surrogate_eval_tc_limit(const float* params, const float* X, size_t n, float* Y, int gelu_mode,
+                                 long long wait_limit, void* stream) {
     TVGB_CHECK_ARG(params && X && Y, "tvgb_surrogate_eval_tc: NULL pointer");
     TVGB_CHECK_ARG(gelu_mode == 0 || gelu_mode == 1, "tvgb_surrogate_eval_tc: gelu_mode must be 0 or 1");
+    TVGB_CHECK_ARG(wait_limit <= (long long)TC_WAIT_LIMIT,
+                   "tvgb_surrogate_eval_tc_limit: wait_limit above the default %u", TC_WAIT_LIMIT);
+    const uint32_t limit = wait_limit < 0 ? TC_WAIT_LIMIT : uint32_t(wait_limit);
     if (n == 0) return TVGB_OK;
     cudaStream_t st = as_stream(stream);
     DevArray dx, dy;
@@ -611,7 +620,7 @@ int tvgb_surrogate_eval_tc(const float* params, const float* X, size_t n, float*
     int* err = reinterpret_cast<int*>(static_cast<char*>(net.p) + TC_IMG_BYTES);
     TVGB_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
     TVGB_TRY(sur_upload_tc(params, net.p, st));
-    TVGB_TRY(sur_eval_tc_device(net.p, dx.get<float>(), n, dy.get<float>(), gelu_mode, err, st));
+    TVGB_TRY(sur_eval_tc_device(net.p, dx.get<float>(), n, dy.get<float>(), gelu_mode, err, st, limit));
     int herr = 0;
     TVGB_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st));
     TVGB_TRY(dy.finish());

@@ -47,7 +47,8 @@ int sur_upload(const float* params, uint2* frag_dev, float* bias_dev, cudaStream
 int sur_eval_device(const uint2* frag, const float* bias, const float* X, size_t n, float* Y, cudaStream_t s);
 // the tcgen05 network (sur_tc.cuh): weight image upload and evaluation
 int sur_upload_tc(const float* params, void* img_dev, cudaStream_t s);
-int sur_eval_tc_device(const void* img, const float* X, size_t n, float* Y, int gelu_mode, int* err, cudaStream_t s);
+int sur_eval_tc_device(const void* img, const float* X, size_t n, float* Y, int gelu_mode, int* err, cudaStream_t s,
+                       uint32_t wait_limit = 1u << 24);
 
 // window rule of the reference's Python layer (tensorvote_tk.cu:88-95)
 inline unsigned auto_window(float s1, float s2) {

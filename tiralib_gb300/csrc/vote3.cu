@@ -1721,7 +1721,7 @@ __global__ void __launch_bounds__(128) k_vote3_surtc(SurVoteArgs a) {
                     const uint32_t in8[8] = {pack_bf16x2(oxf * il, oyf * il), pack_bf16x2(ozf * il, B.x),
                                              pack_bf16x2(B.y, B.z), pack_bf16x2(1.0f, 1.0f),
                                              pack_bf16x2(1.0f, 0.0f), 0u, 0u, 0u};
-                    tc::tmem_st8(tA, in8);
+                    if (!tcs.failed) tc::tmem_st8(tA, in8);
                     if (!sur_tc_layer<1>(tcs)) { ok = false; break; }
                     // the exact stick vote while layer 1 runs
                     if (STICK)
@@ -1732,7 +1732,7 @@ __global__ void __launch_bounds__(128) k_vote3_surtc(SurVoteArgs a) {
                     sur_tc_hidden<1>(tcs);
                     if (!sur_tc_layer<3>(tcs)) { ok = false; break; }
                     sur_tc_hidden<1>(tcs);
-                    if (!sur_tc_layer<4>(tcs)) { ok = false; break; }
+                    if (!sur_tc_layer<4>(tcs) || tcs.failed) { ok = false; break; }
                     uint32_t r[16];
                     tc::tmem_ld16(tD, r);
                     const float w = B.w * ta.x;                      // plate scale x c1(|o|)

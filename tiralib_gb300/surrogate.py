@@ -111,17 +111,19 @@ def train(params, X, T, batch=8192, steps=2000, lr=2e-3, history=True):
 _GELU = {"fp32": 0, "bf16": 1}
 
 
-def evaluate(params, X, engine="tcgen05", gelu="bf16"):
+def evaluate(params, X, engine="tcgen05", gelu="bf16", wait_limit=None):
     """The network's outputs (n x 8, 6 used) on the tensor cores.  engine
     "tcgen05" (tensor memory; gelu "bf16", the packed arithmetic the network
     is trained with and the vote uses, or "fp32") or "mma" (warp-level
-    mma.sync, GELU in FP32; a cross-check of the tcgen05 path)."""
+    mma.sync, GELU in FP32; a cross-check of the tcgen05 path).  wait_limit
+    (tcgen05 only) bounds each layer's wait for its MMAs in mbarrier polls;
+    None is the library's default, and a wait that runs out raises TvgbError."""
     X = _api._check_f32(X, "X")
     Y = _api._empty_like_kind(X, (int(X.shape[0]), 8))
     P = _api._ptr(_api._check_f32(params, "params"))
     if engine == "tcgen05":
-        _api.call("tvgb_surrogate_eval_tc", P, _api._ptr(X), int(X.shape[0]), _api._ptr(Y), _GELU[gelu],
-                  _api._stream_for(X, Y))
+        _api.call("tvgb_surrogate_eval_tc_limit", P, _api._ptr(X), int(X.shape[0]), _api._ptr(Y), _GELU[gelu],
+                  -1 if wait_limit is None else int(wait_limit), _api._stream_for(X, Y))
     elif engine == "mma":
         if gelu != "fp32":
             raise ValueError("the mma engine computes the GELU in FP32 only")
