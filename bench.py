@@ -353,19 +353,36 @@ def parse_profile(text):
     return out
 
 
-def profiled_traffic(kernel, workload="c2"):
-    """DRAM bytes per launch from the committed ncu summary of that kernel on
-    that workload (profiles/<kernel>_<workload>.md), if one exists."""
+def profiled_traffic(kernel, workload="c2", units=None):
+    """DRAM traffic per launch of a kernel, as recorded in its committed ncu
+    summary (profiles/<kernel>_<workload>.md), not measured in this run.  The
+    summary holds `dram_bytes_per_launch: <bytes>` and `traffic_source:
+    <capture, date>`; `dram_units_per_launch: <n>` when the capture ran a
+    smaller case, whose traffic is then scaled by units / n (traffic grows in
+    proportion to the units processed).  Returns {"traffic": bytes or None,
+    "traffic_source": text or None}."""
+    out = {"traffic": None, "traffic_source": None}
     path = os.path.join(HERE, "profiles", f"{kernel}_{workload}.md")
     if not os.path.exists(path):
-        return None
+        return out
+    fields = {}
     for line in open(path):
-        if line.strip().startswith("dram_bytes_per_launch:"):
-            try:
-                return float(line.split(":", 1)[1])
-            except ValueError:
-                return None
-    return None
+        line = line.strip()
+        for key in ("dram_bytes_per_launch", "dram_units_per_launch", "traffic_source"):
+            if line.startswith(key + ":"):
+                fields[key] = line.split(":", 1)[1].strip()
+    try:
+        t = float(fields["dram_bytes_per_launch"])
+    except (KeyError, ValueError):
+        return out
+    src = f"profiles/{kernel}_{workload}.md: {fields.get('traffic_source', 'ncu capture')}"
+    if units and "dram_units_per_launch" in fields:
+        cap = float(fields["dram_units_per_launch"])
+        t *= units / cap
+        src += f"; scaled by {units:.4g} / {cap:.4g} units"
+    out["traffic"] = t
+    out["traffic_source"] = src
+    return out
 
 
 def run_ours(args, rank, world, local_rank):
@@ -503,7 +520,7 @@ def run_ours(args, rank, world, local_rank):
                     "unit": "TFLOP/s", "frac": achieved / pk["nominal"], "peak_source": pk["source"],
                     "peak_measured_fma_chains": pk["measured"], "frac_of_measured_fma_chains":
                         achieved / pk["measured"],
-                    "traffic": profiled_traffic("k_vote3_fast", args.config),
+                    **profiled_traffic("k_vote3_fast", args.config),
                     "flops_per_launch": flops, "avg_launch_ms": avg_s * 1e3,
                     "share_of_step": (tot_ms / (np.sum(times))) if np.sum(times) else None}
 
@@ -751,20 +768,18 @@ def run_c3(args, rank, world, local_rank):
         tv.api.call("tvgb_eig3", tv.api._ptr(mn), 9, n, tv.api._ptr(evn), tv.api._ptr(vecn), 1, 1, None, None)
         e2e.append(time.perf_counter() - t0)
     peaks = measured_peaks()
-    # the precise call is k_eig3 (FP32 pass) + k_eig3_refine (FP64 queue) per chunk of 2^26 tensors:
-    # its roofline is the call's algorithmic bytes over the two kernels' time per call
+    # the precise call is one k_eig3 launch (FP32 solve, FP64 refinement of the flagged tensors from the tile
+    # in shared memory): its roofline is the call's algorithmic bytes over the kernel's time per call
     nl, tot = prof.get("k_eig3", (0, 0.0))
-    _, tot_r = prof.get("k_eig3_refine", (0, 0.0))
     bytes_per = 36 + 12 + 36
     roof = None
     if nl:
-        avg = (tot + tot_r) / args.steps / 1e3
+        avg = tot / args.steps / 1e3
         ach = n * bytes_per / avg / 1e9
-        roof = {"bound": "hbm", "kernel": "k_eig3 + k_eig3_refine (precise, per call)", "achieved": ach,
+        roof = {"bound": "hbm", "kernel": "k_eig3 (precise, per call)", "achieved": ach,
                 "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": ach / peaks["hbm_gbs"],
-                "peak_source": peaks["source"], "traffic": profiled_traffic("k_eig3", "c3"),
-                "bytes_per_tensor": bytes_per, "avg_call_kernel_ms": avg * 1e3,
-                "fp32_pass_ms": tot / args.steps, "fp64_pass_ms": tot_r / args.steps}
+                "peak_source": peaks["source"], "bytes_per_tensor": bytes_per, "avg_call_kernel_ms": avg * 1e3}
+        roof.update(profiled_traffic("k_eig3", "c3", n))
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         v, th, desc = cpu_eigen_sample()
@@ -939,7 +954,7 @@ def run_c1(args, rank, world, local_rank):
                 "frac": ach / pk["nominal"], "peak_measured_fma_chains": pk["measured"],
                 "frac_of_measured_fma_chains": ach / pk["measured"],
                 "flops_per_pair": 30, "avg_launch_ms": avg * 1e3, "peak_source": pk["source"],
-                "traffic": profiled_traffic("k_vote2_tk", "c1")}
+                **profiled_traffic("k_vote2_tk", "c1")}
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         from oracle import oracle as O

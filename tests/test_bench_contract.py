@@ -4,6 +4,7 @@ benchmark contract in its JSON line, and under a multi-rank launch only rank
 0 prints.  The roofline's pair count is exact, and the kernel summaries the
 bench reads its DRAM traffic from carry that figure."""
 import json
+import re
 import os
 import subprocess
 import sys
@@ -71,9 +72,14 @@ def test_pair_count_is_exact():
 
 def test_profiles_carry_the_traffic_the_bench_reads():
     """Every kernel summary the bench takes its DRAM traffic from keeps a
-    machine-readable per-launch figure."""
+    machine-readable per-launch figure and says where it came from (the
+    capture and its date), and the bench line carries that source beside the
+    figure."""
     import bench
     for kernel, workload in [("k_vote3_fast", "c2"), ("k_vote3_fast", "c4"), ("k_eig3", "c3"),
                              ("k_vote2_tk", "c1"), ("k_st3", "c2")]:
         t = bench.profiled_traffic(kernel, workload)
-        assert t is not None and t > 0, (kernel, workload)
+        assert t["traffic"] is not None and t["traffic"] > 0, (kernel, workload)
+        assert t["traffic_source"].startswith(f"profiles/{kernel}_{workload}.md: "), t
+        assert re.search(r"20\d\d-\d\d-\d\d", t["traffic_source"]), t
+    assert bench.profiled_traffic("k_none", "c9") == {"traffic": None, "traffic_source": None}

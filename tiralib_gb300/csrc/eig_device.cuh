@@ -225,47 +225,53 @@ __device__ __forceinline__ void from_spherical_d(float theta, float phi, float* 
 // plane projection, the 2x2 solve and the frame are redone in FP64.
 
 // the plane normal to unit w, the 2x2 problem on it, Rayleigh quotients;
-// A = (xx, xy, xz, yy, yz, zz).  Outputs lx <= ly with vectors x, y; lw.
-template <class T>
-__device__ __forceinline__ void complement_solve(const T* A, const T* w, T& lx, T& ly, T* x, T* y, T& lw, T& rw) {
-    T t[3];
-    const T aw0 = fabs(w[0]), aw1 = fabs(w[1]), aw2 = fabs(w[2]);
-    if (aw0 <= aw1 && aw0 <= aw2) { t[0] = 1; t[1] = 0; t[2] = 0; }
-    else if (aw1 <= aw2) { t[0] = 0; t[1] = 1; t[2] = 0; }
-    else { t[0] = 0; t[1] = 0; t[2] = 1; }
-    T U[3] = {w[1] * t[2] - w[2] * t[1], w[2] * t[0] - w[0] * t[2], w[0] * t[1] - w[1] * t[0]};
-    const T nu = T(1) / sqrt(U[0] * U[0] + U[1] * U[1] + U[2] * U[2]);
+// A = (xx, xy, xz, yy, yz, zz), entries scaled into [-2, 2].  Outputs lx <= ly
+// with vectors x, y; lw and the squared residual rw of (lw, w).  Unit
+// lengths come from the hardware reciprocal square root (2 ulp): the FP32
+// results carry ~1e-7 relative rounding either way.
+__device__ __forceinline__ void complement_solve(const float* A, const float* w, float& lx, float& ly, float* x,
+                                                 float* y, float& lw, float& rw) {
+    // U = w x e_k for the axis k of the smallest |w_k| (two non-zero components), V = w x U
+    const float aw0 = fabsf(w[0]), aw1 = fabsf(w[1]), aw2 = fabsf(w[2]);
+    float U[3];
+    if (aw0 <= aw1 && aw0 <= aw2) { U[0] = 0.0f; U[1] = w[2]; U[2] = -w[1]; }
+    else if (aw1 <= aw2) { U[0] = -w[2]; U[1] = 0.0f; U[2] = w[0]; }
+    else { U[0] = w[1]; U[1] = -w[0]; U[2] = 0.0f; }
+    const float nu = rsqrtf(fmaf(U[0], U[0], fmaf(U[1], U[1], U[2] * U[2])));
     U[0] *= nu; U[1] *= nu; U[2] *= nu;
-    const T V[3] = {w[1] * U[2] - w[2] * U[1], w[2] * U[0] - w[0] * U[2], w[0] * U[1] - w[1] * U[0]};
-    auto mv = [&](const T* v, T* r) {
-        r[0] = A[0] * v[0] + A[1] * v[1] + A[2] * v[2];
-        r[1] = A[1] * v[0] + A[3] * v[1] + A[4] * v[2];
-        r[2] = A[2] * v[0] + A[4] * v[1] + A[5] * v[2];
+    const float V[3] = {w[1] * U[2] - w[2] * U[1], w[2] * U[0] - w[0] * U[2], w[0] * U[1] - w[1] * U[0]};
+    auto mv = [&](const float* v, float* r) {
+        r[0] = fmaf(A[0], v[0], fmaf(A[1], v[1], A[2] * v[2]));
+        r[1] = fmaf(A[1], v[0], fmaf(A[3], v[1], A[4] * v[2]));
+        r[2] = fmaf(A[2], v[0], fmaf(A[4], v[1], A[5] * v[2]));
     };
-    T AU[3], AV[3], AW[3];
+    float AU[3], AV[3], AW[3];
     mv(U, AU); mv(V, AV); mv(w, AW);
-    const T h00 = U[0] * AU[0] + U[1] * AU[1] + U[2] * AU[2];
-    const T h01 = U[0] * AV[0] + U[1] * AV[1] + U[2] * AV[2];
-    const T h11 = V[0] * AV[0] + V[1] * AV[1] + V[2] * AV[2];
-    lw = w[0] * AW[0] + w[1] * AW[1] + w[2] * AW[2];
+    const float h00 = fmaf(U[0], AU[0], fmaf(U[1], AU[1], U[2] * AU[2]));
+    const float h01 = fmaf(U[0], AV[0], fmaf(U[1], AV[1], U[2] * AV[2]));
+    const float h11 = fmaf(V[0], AV[0], fmaf(V[1], AV[1], V[2] * AV[2]));
+    lw = fmaf(w[0], AW[0], fmaf(w[1], AW[1], w[2] * AW[2]));
     {   // squared residual of the isolated pair (lw, w)
-        const T r0 = AW[0] - lw * w[0], r1 = AW[1] - lw * w[1], r2 = AW[2] - lw * w[2];
-        rw = r0 * r0 + r1 * r1 + r2 * r2;
+        const float r0 = fmaf(-lw, w[0], AW[0]), r1 = fmaf(-lw, w[1], AW[1]), r2 = fmaf(-lw, w[2], AW[2]);
+        rw = fmaf(r0, r0, fmaf(r1, r1, r2 * r2));
     }
-    T cs = 1, sn = 0;
-    if (h01 != T(0)) {     // Jacobi rotation zeroing h01
-        const T th = (h11 - h00) / (T(2) * h01);
-        const T tt = (th >= T(0) ? T(1) : T(-1)) / (fabs(th) + sqrt(th * th + T(1)));
-        cs = T(1) / sqrt(tt * tt + T(1));
+    float cs = 1.0f, sn = 0.0f;
+    if (h01 != 0.0f) {     // Jacobi rotation zeroing h01: tt = tan of the angle, |tt| <= 1
+        const float th = __fdividef(h11 - h00, 2.0f * h01);
+        const float ath = fabsf(th);
+        // for |th| > 2^60, th^2 + 1 would overflow; tt -> 1 / (2 th) there
+        const float den = ath > 1.0e18f ? 2.0f * ath : ath + sqrtf(fmaf(th, th, 1.0f));
+        const float tt = copysignf(__fdividef(1.0f, den), th);
+        cs = rsqrtf(fmaf(tt, tt, 1.0f));
         sn = tt * cs;
     }
-    for (int k = 0; k < 3; ++k) { x[k] = cs * U[k] - sn * V[k]; y[k] = sn * U[k] + cs * V[k]; }
-    T Ax[3], Ay[3];
+    for (int k = 0; k < 3; ++k) { x[k] = cs * U[k] - sn * V[k]; y[k] = fmaf(sn, U[k], cs * V[k]); }
+    float Ax[3], Ay[3];
     mv(x, Ax); mv(y, Ay);
-    lx = x[0] * Ax[0] + x[1] * Ax[1] + x[2] * Ax[2];
-    ly = y[0] * Ay[0] + y[1] * Ay[1] + y[2] * Ay[2];
+    lx = fmaf(x[0], Ax[0], fmaf(x[1], Ax[1], x[2] * Ax[2]));
+    ly = fmaf(y[0], Ay[0], fmaf(y[1], Ay[1], y[2] * Ay[2]));
     if (lx > ly) {
-        T tmp;
+        float tmp;
         for (int k = 0; k < 3; ++k) { tmp = x[k]; x[k] = y[k]; y[k] = tmp; }
         tmp = lx; lx = ly; ly = tmp;
     }
@@ -297,6 +303,8 @@ __device__ __forceinline__ void assemble(bool iso_high, T lw, const T* w, T lx, 
 // are set and the return value selects the FP64 phase: 1 = the remaining
 // pair is closer than 1e-4 |lambda_max| (project onto the plane in FP64),
 // 2 = Smith's formula isolated no eigenvalue (a near-triple cluster: Jacobi).
+// Only the isolated eigenvalue is taken from Smith's formula: the largest
+// when det(A - qI) >= 0 (phi <= pi/6), else the smallest.
 __device__ __forceinline__ int eig3_precise_fp32(float a, float b, float c, float d, float e, float f, float* ev,
                                                  float* v0, float* v1, float* v2, float* w, bool& iso_high) {
     const float amax = fmaxf(fmaxf(fmaxf(fabsf(a), fabsf(b)), fmaxf(fabsf(c), fabsf(d))), fmaxf(fabsf(e), fabsf(f)));
@@ -309,17 +317,44 @@ __device__ __forceinline__ int eig3_precise_fp32(float a, float b, float c, floa
     int ex;
     frexpf(amax, &ex);
     const float sc = ldexpf(1.0f, 1 - ex), unsc = ldexpf(1.0f, ex - 1);   // entries scaled into [1, 2)
-    const float A[6] = {a * sc, b * sc, d * sc, c * sc, e * sc, f * sc};
-    float l[3];
-    eval3_d(A[0], A[1], A[3], A[2], A[4], A[5], l[0], l[1], l[2]);
-    iso_high = (l[2] - l[1]) >= (l[1] - l[0]);
-    evec3_0_d(A[0], A[1], A[3], A[2], A[4], A[5], iso_high ? l[2] : l[0], w);
-    float wn = w[0] * w[0] + w[1] * w[1] + w[2] * w[2];
-    if (!(wn > 0.25f)) { w[0] = 0; w[1] = 0; w[2] = 1; wn = 1; }   // cofactors vanished: A ~ l I
-    const float iw = rsqrtf(wn);
-    w[0] *= iw; w[1] *= iw; w[2] *= iw;
+    const float A[6] = {a * sc, b * sc, d * sc, c * sc, e * sc, f * sc};   // xx xy xz yy yz zz
+    // Smith: A = qI + pB, det(B) / 2 = cos(3 phi)
+    const float q = (A[0] + A[3] + A[5]) * (1.0f / 3.0f);
+    const float aq = A[0] - q, cq = A[3] - q, fq = A[5] - q;
+    const float p6 = fmaf(aq, aq, fmaf(cq, cq, fmaf(fq, fq, 2.0f * fmaf(A[1], A[1], fmaf(A[2], A[2], A[4] * A[4]))))) *
+                     (1.0f / 6.0f);
+    float l = q;
+    if (p6 > 0.0f) {
+        const float rp = rsqrtf(p6), p = p6 * rp;
+        const float det = aq * fmaf(cq, fq, -A[4] * A[4]) - A[1] * fmaf(A[1], fq, -A[4] * A[2]) +
+                          A[2] * fmaf(A[1], A[4], -cq * A[2]);
+        const float r = fminf(fmaxf(0.5f * det * (rp * rp * rp), -1.0f), 1.0f);
+        iso_high = r >= 0.0f;
+        const float phi = acosf(r) * (1.0f / 3.0f);
+        l = fmaf(2.0f * p, cosf(iso_high ? phi : phi + 2.0f * TVGB_PI_F / 3.0f), q);
+    }
+    // w: the largest cofactor row of A - l I (eigen.h's evec3_symmetric_0 rule)
+    {
+        const float m00 = A[0] - l, m11 = A[3] - l, m22 = A[5] - l, m01 = A[1], m02 = A[2], m12 = A[4];
+        const float c0[3] = {m11 * m22 - m12 * m12, m12 * m02 - m01 * m22, m01 * m12 - m11 * m02};
+        const float c1[3] = {m02 * m12 - m01 * m22, m00 * m22 - m02 * m02, m01 * m02 - m00 * m12};
+        const float c2[3] = {m01 * m12 - m02 * m11, m02 * m01 - m00 * m12, m00 * m11 - m01 * m01};
+        const float r0 = fmaf(c0[0], c0[0], fmaf(c0[1], c0[1], c0[2] * c0[2]));
+        const float r1 = fmaf(c1[0], c1[0], fmaf(c1[1], c1[1], c1[2] * c1[2]));
+        const float r2 = fmaf(c2[0], c2[0], fmaf(c2[1], c2[1], c2[2] * c2[2]));
+        const bool s0 = r0 >= r1 && r0 >= r2, s1 = !s0 && r1 >= r2;
+        const float rb = s0 ? r0 : (s1 ? r1 : r2);
+        if (rb > 1e-12f) {
+            const float iw = rsqrtf(rb);
+            w[0] = (s0 ? c0[0] : (s1 ? c1[0] : c2[0])) * iw;
+            w[1] = (s0 ? c0[1] : (s1 ? c1[1] : c2[1])) * iw;
+            w[2] = (s0 ? c0[2] : (s1 ? c1[2] : c2[2])) * iw;
+        } else {                       // cofactors vanished: A ~ l I
+            w[0] = 0.0f; w[1] = 0.0f; w[2] = 1.0f;
+        }
+    }
     float lx, ly, lw, rw, x[3], y[3];
-    complement_solve<float>(A, w, lx, ly, x, y, lw, rw);
+    complement_solve(A, w, lx, ly, x, y, lw, rw);
     if (rw > 1e-10f) return 2;      // w's residual well above FP32 rounding
     const float lm = fmaxf(fmaxf(fabsf(lx), fabsf(ly)), fabsf(lw));
     if ((ly - lx) < 1e-4f * lm) return 1;

@@ -13,12 +13,15 @@
 // while the current one is solved.
 //
 // Precise mode: a scale-invariant FP32 solve for every tensor; tensors whose
-// remaining pair is closer than 1e-4 |lambda_max| are appended to a compact
-// queue in global memory (one atomic per block), and a second kernel
-// finishes the queue in FP64 at full occupancy, so the FP64 pipe only sees
-// flagged tensors and no lane waits for it.  (Finishing them inside the
-// block left ~3/4 of its warps waiting at a barrier.)  Both kernels run per
-// chunk of at most 2^26 tensors, which bounds the queue.
+// remaining pair is closer than 1e-4 |lambda_max| are appended to a queue in
+// shared memory, and after a barrier the block's first threads finish the
+// queue in FP64, one flagged tensor per thread, reading the tensor from the
+// tile still in shared memory and writing their results into the tile's
+// output buffers before the coalesced store.  Each tensor is read from HBM
+// once and each result written once, and the FP64 pipe only sees flagged
+// tensors (27% of the C3 recipe's), packed into whole warps.  While a block
+// drains its queue with a few warps, the other resident blocks keep the SM
+// issuing FP32 work.
 #include "tvgb_common.cuh"
 #include "eig_device.cuh"
 #include <algorithm>
@@ -27,6 +30,11 @@
 namespace tvgb {
 
 constexpr int EIG_BLOCK = 256;
+// resident blocks per SM the precise kernel is compiled for: its FP64 phase
+// would otherwise take the register count past 64 per thread
+#ifndef TVGB_EIG_MINB
+#define TVGB_EIG_MINB 4
+#endif
 
 // in_layout: 9 (mat3 AoS), 6 (sym6 AoS), 60 (sym6 planes)
 template <int IN_LAYOUT>
@@ -73,22 +81,22 @@ __device__ __forceinline__ void store_tile(float* __restrict__ dst, const float*
 
 // EVEC_FMT: 0 none, 1 cartesian (9), 2 spherical (6).  EVALS_IN: take the
 // eigenvalues from `evals_in` (the reference's evecs3spherical contract).
-// queue record of a tensor left to the FP64 phase: (index in its chunk |
-// code << 28 | isolated-high << 30, w0, w1, w2)
-constexpr size_t EIG_CHUNK = size_t(1) << 26;
-
+// Shared-memory queue record of a tensor left to the FP64 phase: (slot in the
+// tile | code << 28 | isolated-high << 30, w0, w1, w2).
 template <int IN_LAYOUT, int EVEC_FMT, bool PRECISE, bool EVALS_IN>
-__global__ void __launch_bounds__(EIG_BLOCK) k_eig3(const float* __restrict__ in, size_t n, size_t first, size_t last,
+__global__ void __launch_bounds__(EIG_BLOCK, PRECISE ? TVGB_EIG_MINB : 1) k_eig3(const float* __restrict__ in, size_t n, size_t first, size_t last,
                                                       const float* __restrict__ evals_in, float* __restrict__ evals,
-                                                      float* __restrict__ evecs, uint4* __restrict__ queue,
-                                                      unsigned* __restrict__ qcount, int aligned_in, int aligned_out) {
+                                                      float* __restrict__ evecs,
+                                                      unsigned long long* __restrict__ n_refined, int aligned_in,
+                                                      int aligned_out) {
     constexpr int NF = IN_LAYOUT == 9 ? 9 : 6;
     constexpr int NV = EVEC_FMT == 1 ? 9 : (EVEC_FMT == 2 ? 6 : 0);
     __shared__ __align__(16) float s_in2[2][EIG_BLOCK * NF];   // the current tile and the next one
     __shared__ __align__(16) float s_ev[EIG_BLOCK * 3];
     __shared__ __align__(16) float s_vec[EIG_BLOCK * 9];
     __shared__ uint4 s_q[PRECISE ? EIG_BLOCK : 1];
-    __shared__ unsigned s_qn, s_qbase;
+    __shared__ unsigned s_qn;
+    unsigned refined = 0;   // thread 0: flagged tensors of this block
 
     const size_t stride = size_t(gridDim.x) * EIG_BLOCK;
     // tile at `base` into buffer `buf`: asynchronous when full, aligned and AoS
@@ -122,13 +130,10 @@ __global__ void __launch_bounds__(EIG_BLOCK) k_eig3(const float* __restrict__ in
                 float w[3];
                 bool hi;
                 const int code = eig3_precise_fp32(a, b, c, d, e, f, ev, v, v + 3, v + 6, w, hi);
-                if (code) {   // left to the FP64 kernel; the FP32 result is written meanwhile
-                    const unsigned key = unsigned(base + t - first) | (unsigned(code) << 28) | ((hi ? 1u : 0u) << 30);
+                if (code) {   // left to the FP64 phase below, which overwrites this slot's results
+                    const unsigned key = unsigned(t) | (unsigned(code) << 28) | ((hi ? 1u : 0u) << 30);
                     s_q[atomicAdd(&s_qn, 1u)] = make_uint4(key, __float_as_uint(w[0]), __float_as_uint(w[1]),
                                                            __float_as_uint(w[2]));
-                    v[0] = w[0]; v[1] = w[1]; v[2] = w[2];
-                    v[3] = v[4] = v[5] = v[6] = v[7] = v[8] = 0.0f;
-                    ev[0] = ev[1] = ev[2] = 0.0f;
                 }
             } else {
                 if (EVALS_IN) { ev[0] = s_ev[t * 3]; ev[1] = s_ev[t * 3 + 1]; ev[2] = s_ev[t * 3 + 2]; }
@@ -140,11 +145,25 @@ __global__ void __launch_bounds__(EIG_BLOCK) k_eig3(const float* __restrict__ in
                 for (int k = 0; k < 9; ++k) s_vec[t * 9 + k] = v[k];
         }
         __syncthreads();
-        if (PRECISE) {   // append this tile's flagged tensors to the chunk's queue
+        if (PRECISE) {   // the tile's flagged tensors in FP64, packed into the first warps
             const unsigned qn = s_qn;
-            if (threadIdx.x == 0 && qn) s_qbase = atomicAdd(qcount, qn);
+            if (threadIdx.x == 0) refined += qn;
+            if (threadIdx.x < qn) {
+                const uint4 r = s_q[threadIdx.x];
+                const int slot = int(r.x & 0x0FFFFFFFu);
+                const int code = int((r.x >> 28) & 3u);
+                const bool hi = (r.x >> 30) & 1u;
+                const float w[3] = {__uint_as_float(r.y), __uint_as_float(r.z), __uint_as_float(r.w)};
+                const float* m = s_in + slot * NF;
+                float a, b, c, d, e, f;
+                if (NF == 9) { a = m[0]; b = m[1]; d = m[2]; c = m[4]; e = m[5]; f = m[8]; }
+                else { a = m[0]; b = m[1]; d = m[2]; c = m[3]; e = m[4]; f = m[5]; }
+                float ev[3], v[9];
+                eig3_precise_fp64(a, b, c, d, e, f, w, hi, code, ev, v, v + 3, v + 6);
+                s_ev[slot * 3] = ev[0]; s_ev[slot * 3 + 1] = ev[1]; s_ev[slot * 3 + 2] = ev[2];
+                for (int k = 0; k < 9; ++k) s_vec[slot * 9 + k] = v[k];
+            }
             __syncthreads();
-            for (unsigned j = threadIdx.x; j < qn; j += EIG_BLOCK) queue[s_qbase + j] = s_q[j];
         }
         if (EVEC_FMT == 2) {
             // spherical output, packed 6 per tensor into the front of s_vec
@@ -166,45 +185,7 @@ __global__ void __launch_bounds__(EIG_BLOCK) k_eig3(const float* __restrict__ in
         if (NV && evecs) store_tile(evecs + base * NV, s_vec, cnt * NV, aligned_out, full);
         __syncthreads();
     }
-}
-
-// The FP64 phase over a chunk's queue: one thread per flagged tensor, the
-// tensor re-read from the input, results written in place of the FP32 ones.
-template <int IN_LAYOUT, int EVEC_FMT>
-__global__ void __launch_bounds__(256) k_eig3_refine(const float* __restrict__ in, size_t n, size_t first,
-                                                     const uint4* __restrict__ queue, const unsigned* __restrict__ qcount,
-                                                     float* __restrict__ evals, float* __restrict__ evecs,
-                                                     unsigned long long* __restrict__ n_refined) {
-    const unsigned qn = *qcount;
-    if (n_refined && blockIdx.x == 0 && threadIdx.x == 0 && qn) atomicAdd(n_refined, (unsigned long long)qn);
-    for (size_t q = size_t(blockIdx.x) * blockDim.x + threadIdx.x; q < qn; q += size_t(gridDim.x) * blockDim.x) {
-        const uint4 r = queue[q];
-        const size_t i = first + (r.x & 0x0FFFFFFFu);
-        const int code = int((r.x >> 28) & 3u);
-        const bool hi = (r.x >> 30) & 1u;
-        const float w[3] = {__uint_as_float(r.y), __uint_as_float(r.z), __uint_as_float(r.w)};
-        float a, b, c, d, e, f;
-        if (IN_LAYOUT == 9) {
-            const float* m = in + i * 9;
-            a = m[0]; b = m[1]; d = m[2]; c = m[4]; e = m[5]; f = m[8];
-        } else if (IN_LAYOUT == 6) {
-            const float* m = in + i * 6;
-            a = m[0]; b = m[1]; d = m[2]; c = m[3]; e = m[4]; f = m[5];
-        } else {
-            a = in[i]; b = in[n + i]; d = in[2 * n + i]; c = in[3 * n + i]; e = in[4 * n + i]; f = in[5 * n + i];
-        }
-        float ev[3], v[9];
-        eig3_precise_fp64(a, b, c, d, e, f, w, hi, code, ev, v, v + 3, v + 6);
-        if (evals) { evals[i * 3] = ev[0]; evals[i * 3 + 1] = ev[1]; evals[i * 3 + 2] = ev[2]; }
-        if (EVEC_FMT == 1 && evecs)
-            for (int k = 0; k < 9; ++k) evecs[i * 9 + k] = v[k];
-        if (EVEC_FMT == 2 && evecs) {
-            float th, ph;
-            to_spherical_d(v, th, ph); evecs[i * 6] = th; evecs[i * 6 + 1] = ph;
-            to_spherical_d(v + 3, th, ph); evecs[i * 6 + 2] = th; evecs[i * 6 + 3] = ph;
-            to_spherical_d(v + 6, th, ph); evecs[i * 6 + 4] = th; evecs[i * 6 + 5] = ph;
-        }
-    }
+    if (PRECISE && n_refined && threadIdx.x == 0 && refined) atomicAdd(n_refined, (unsigned long long)refined);
 }
 
 __global__ void k_eval2(const float4* __restrict__ m4, size_t n, float2* __restrict__ ev2) {
@@ -276,38 +257,13 @@ static int launch_eig3_t(const float* in, size_t n, const float* ev_in, float* e
                          cudaStream_t s) {
     const int ai = (reinterpret_cast<uintptr_t>(in) % 16) == 0;
     const int ao = (!ev || reinterpret_cast<uintptr_t>(ev) % 16 == 0) && (!vec || reinterpret_cast<uintptr_t>(vec) % 16 == 0);
-    if (!PR) {
+    {
         KernelTimer kt_("k_eig3", s);
         k_eig3<IL, EF, PR, EI><<<resident_grid(k_eig3<IL, EF, PR, EI>, EIG_BLOCK, n), EIG_BLOCK, 0, s>>>(
-            in, n, 0, n, ev_in, ev, vec, nullptr, nullptr, ai, ao);
+            in, n, 0, n, ev_in, ev, vec, PR ? nref : nullptr, ai, ao);
         kt_.stop();
-        TVGB_LAUNCHED();
-        return TVGB_OK;
     }
-    // precise: per chunk, the FP32 pass (queueing) then the FP64 pass over the queue
-    const size_t qcap = std::min(n, EIG_CHUNK);
-    Scratch sq;
-    TVGB_TRY(sq.alloc(qcap * sizeof(uint4) + 16, s));
-    uint4* queue = sq.get<uint4>();
-    unsigned* qcount = reinterpret_cast<unsigned*>(queue + qcap);
-    for (size_t first = 0; first < n; first += EIG_CHUNK) {
-        const size_t last = std::min(n, first + EIG_CHUNK);
-        TVGB_CUDA(cudaMemsetAsync(qcount, 0, sizeof(unsigned), s));
-        {
-            KernelTimer kt_("k_eig3", s);
-            k_eig3<IL, EF, PR, EI><<<resident_grid(k_eig3<IL, EF, PR, EI>, EIG_BLOCK, last - first), EIG_BLOCK, 0, s>>>(
-                in, n, first, last, ev_in, ev, vec, queue, qcount, ai, ao);
-            kt_.stop();
-        }
-        TVGB_LAUNCHED();
-        {
-            KernelTimer kt_("k_eig3_refine", s);
-            k_eig3_refine<IL, EF><<<resident_grid(k_eig3_refine<IL, EF>, 256, last - first), 256, 0, s>>>(
-                in, n, first, queue, qcount, ev, vec, nref);
-            kt_.stop();
-        }
-        TVGB_LAUNCHED();
-    }
+    TVGB_LAUNCHED();
     return TVGB_OK;
 }
 
