@@ -188,7 +188,8 @@ def cpu_reference_sample(vol, cfg, block=16, seed=0, threads=None, detail=None):
     zz, yy, xx = np.meshgrid(np.arange(hw, hw + block), np.arange(hw, hw + block), np.arange(hw, hw + block),
                              indexing="ij")
     rec = ((zz * S + yy) * S + xx).ravel()
-    out = O.tensorvote3_receivers(m9, rec, cfg["sigma"], 0.0, cfg["w"], 1, samples=cfg["samples"], threads=threads)
+    out = O.tensorvote3_receivers(m9, rec, cfg["sigma"], 0.0, cfg["w"], 1, samples=cfg["samples"], threads=threads,
+                                  is_atv=bool(cfg.get("atv")))
     voted = out.reshape(-1, 9)[rec]
     ev = O.evals3(voted)
     vec = O.evecs3cart(voted, ev)
@@ -215,8 +216,9 @@ def accuracy_against_cpu(detail, cfg, out_d, ev_d, vec_d, threads, precise=None)
     gvec = vec_d[sl].cpu().numpy().reshape(-1, 3, 3).astype(np.float64)
     idx6 = [0, 1, 2, 4, 5, 8]
     c6 = detail["voted"].reshape(-1, 9)[:, idx6].astype(np.float64)
-    f64 = O.tensorvote3_f64(detail["field"], cfg["sigma"], 0.0, cfg["w"], 1, ball=cfg["ball"],
-                            receivers=detail["receivers"], threads=threads).reshape(-1, 6)[detail["receivers"]]
+    f64 = None if cfg.get("atv") else O.tensorvote3_f64(
+        detail["field"], cfg["sigma"], 0.0, cfg["w"], 1, ball=cfg["ball"], receivers=detail["receivers"],
+        threads=threads).reshape(-1, 6)[detail["receivers"]]
     wgt = np.array([1, 2, 2, 1, 2, 1], np.float64)   # off-diagonal entries count twice in the Frobenius norm
 
     def tensor_err(a, ref):
@@ -231,7 +233,7 @@ def accuracy_against_cpu(detail, cfg, out_d, ev_d, vec_d, threads, precise=None)
     ang = np.arccos(cosang)
     out = {"receivers": int(b ** 3), "block_origin_zyx": [int(z0), int(y0), int(x0)],
            "voted_vs_reference_cpu": tensor_err(g6, c6),
-           "voted_vs_fp64": tensor_err(g6, f64),
+           "voted_vs_fp64": tensor_err(g6, f64) if f64 is not None else None,
            "eigenvalues_vs_reference_cpu": {"max": float(ev_rel.max()), "median": float(np.median(ev_rel))},
            "eigenvector_angle_rad_vs_reference_cpu": {"e2_max": float(ang[:, 2].max()),
                                                       "e2_median": float(np.median(ang[:, 2])),
@@ -277,6 +279,7 @@ def config3(args):
     cfg = dict(CONFIGS3[args.config])
     if args.size:
         cfg["n"] = args.size
+    cfg["atv"] = bool(getattr(args, "atv", False))
     return cfg
 
 
@@ -292,6 +295,9 @@ def make_volume(cfg, dev=None):
 
 
 def metric_for(cfg):
+    if cfg.get("atv"):
+        return (f"3D ATV voxels/s ({cfg['name']}: analytical tensor voting, sigma={cfg['sigma']:g}, "
+                f"stick+plate+ball)")
     if cfg["name"] in ("C2", "C4"):
         return METRIC
     return (f"3D tensor-vote voxels/s ({cfg['name']}: sigma={cfg['sigma']:g}, "
@@ -333,13 +339,14 @@ def config_dict(cfg):
     n = cfg["n"]
     terms = "stick+plate+ball" if cfg["ball"] else "stick+plate"
     sheets = f" + {cfg['n_sheets']} sheets" if cfg["n_sheets"] else ""
+    vote = (f"ATV vote (tensorvote.h:710; sigma {cfg['sigma']:g}, w {cfg['w']})" if cfg.get("atv") else
+            f"TK {terms} vote (sigma {cfg['sigma']:g}, w {cfg['w']}, samples {cfg['samples']})")
     return {"workload": f"{cfg['name']}: {n}^3 tube volume{sheets} -> structure tensor (sigma {cfg['sigma_st']:g}) -> "
-                        f"TK {terms} vote (sigma {cfg['sigma']:g}, w {cfg['w']}, samples {cfg['samples']}) -> fused "
-                        "3x3 eigendecomposition",
+                        f"{vote} -> fused 3x3 eigendecomposition",
             "volume": [cfg["n"]] * 3, "tubes": cfg["n_tubes"], "tube_radius": list(cfg["r_range"]),
             "sheets": cfg["n_sheets"], "noise_sd": cfg["noise_sd"], "seed": cfg["seed"],
             "sigma_structure": cfg["sigma_st"], "sigma_vote": cfg["sigma"], "window": cfg["w"],
-            "samples": cfg["samples"], "power": 1, "ball": cfg["ball"],
+            "samples": cfg["samples"], "power": 1, "ball": cfg["ball"], "atv": bool(cfg.get("atv")),
             "path": "plain (exact plate orientation integral, no surrogate)",
             "l2_flush": "256 MiB write between timed steps (outside the events)"}
 
@@ -410,7 +417,7 @@ def run_ours(args, rank, world, local_rank):
     vec_d = torch.empty(dims + (3, 3), device=dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     kw = dict(sigma_st=cfg["sigma_st"], sigma1=cfg["sigma"], w=cfg["w"], samples=cfg["samples"], st_mode="same",
-              out_layout="planes", evecs="cartesian", ball=cfg["ball"])
+              out_layout="planes", evecs="cartesian", ball=cfg["ball"], is_atv=cfg["atv"])
     strong = args.split == "slabs" and world > 1
     if strong:
         # strong scaling: one volume, each rank votes its z-slab (+ halos); no collective on the data path
@@ -513,19 +520,19 @@ def run_ours(args, rank, world, local_rank):
     roofline = None
     if nl:
         avg_s = tot_ms / nl / 1e3
-        flops = pairs_count(dims, cfg["w"] // 2, (z0, z1) if strong else None) * \
-            (FLOPS_PER_PAIR + (FLOPS_PER_PAIR_BALL if cfg["ball"] else 0))
+        per_pair = FLOPS_PER_PAIR + (FLOPS_PER_PAIR_BALL if (cfg["ball"] or cfg["atv"]) else 0)
+        flops = pairs_count(dims, cfg["w"] // 2, (z0, z1) if strong else None) * per_pair
         achieved = flops / avg_s / 1e12
         roofline = {"bound": "fp32", "kernel": "k_vote3_fast", "achieved": achieved, "peak": pk["nominal"],
                     "unit": "TFLOP/s", "frac": achieved / pk["nominal"], "peak_source": pk["source"],
                     "peak_measured_fma_chains": pk["measured"], "frac_of_measured_fma_chains":
                         achieved / pk["measured"],
                     **profiled_traffic("k_vote3_fast", args.config),
-                    "flops_per_launch": flops, "avg_launch_ms": avg_s * 1e3,
+                    "flops_per_launch": flops, "flops_per_pair": per_pair, "avg_launch_ms": avg_s * 1e3,
                     "share_of_step": (tot_ms / (np.sum(times))) if np.sum(times) else None}
 
     sur = None
-    if rank == 0 and world == 1 and not args.no_surrogate and not strong:
+    if rank == 0 and world == 1 and not args.no_surrogate and not strong and not cfg["atv"]:
         sur = surrogate_study(vol_d, cfg, args, dev)
 
     cpu = None
@@ -540,11 +547,12 @@ def run_ours(args, rank, world, local_rank):
             p_vec = torch.empty_like(vec_d)
             tv.pipeline3(vol_d, outputs=(p_out, p_ev, p_vec), parity=False, **kw)
             torch.cuda.synchronize()
-            accuracy = accuracy_against_cpu(detail, cfg, out_d, ev_d, vec_d, th, precise=(p_out, p_ev, p_vec))
+            accuracy = accuracy_against_cpu(detail, cfg, out_d, ev_d, vec_d, th,
+                                            precise=None if cfg["atv"] else (p_out, p_ev, p_vec))
             del p_out, p_ev, p_vec
         cpu = {"value": nrec / t, "unit": "voxels/s", "cores": th, "kind": "port",
                "sample": f"{args.ref_block}^3 interior receivers of the same volume (+ window halo), the reference's "
-                         f"CPU algorithm (stick + {cfg['samples']}-sample plate"
+                         f"CPU algorithm ({'ATV, tensorvote.h:710' if cfg['atv'] else 'stick + ' + str(cfg['samples']) + '-sample plate'}"
                          f"{'; no ball: the reference has no TK ball' if cfg['ball'] else ''}) in oracle/, OpenMP over "
                          "receivers"}
     if rank == 0:
@@ -1041,6 +1049,8 @@ def main():
                     help="c4: 3D pipeline at 384^3, sigma 4, the surrogate study's field (the headline); c2: the same "
                          "at 256^3; c5: 512^3 tubes + sheets, sigma 6, stick + plate + ball (capacity); c3: batched "
                          "3x3 eigen; c1: 2D pipeline")
+    ap.add_argument("--atv", action="store_true", help="c2/c4/c5: vote with ATV (analytical tensor voting, "
+                                                       "tensorvote.h:710) instead of TK")
     ap.add_argument("--split", choices=["replicas", "slabs"], default="replicas",
                     help="N > 1: independent replicas (weak scaling) or z-slabs of one volume (strong scaling)")
     ap.add_argument("--size", type=int, default=0, help="c2/c4/c5: volume edge (default 256/384/512); c3: log2 of "

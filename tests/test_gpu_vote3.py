@@ -83,6 +83,26 @@ def test_vote3_fast_path_matches_oracle(tv, shape, sigma, w, samples):
     assert rel(u6(out), u6(ref)) < TOL
 
 
+@pytest.mark.parametrize("shape,sigma,w", [
+    ((13, 17, 19), 2.0, 9),          # ragged in every axis
+    ((1, 40, 35), 1.0, 3),           # single plane
+    ((5, 6, 40), 3.0, 19),           # window larger than the volume
+    ((20, 24, 36), 2.0, 13),         # several CTAs in every axis
+])
+def test_vote3_atv_fast_path_matches_oracle(tv, shape, sigma, w):
+    """ATV (tensorvote.h:710) on the tiled kernel's stick / plate / ball terms
+    against the oracle's restatement of the reference's per-pair ATV, both
+    through the parity entry point (eigen.h voters with the spherical round
+    trip) and the extended one."""
+    T = spd_field(shape, sum(shape) + 3 * w)
+    ref = oracle_vote3(T, sigma, 0.0, w, 1, is_atv=True)
+    out = np.zeros_like(T)
+    tv.tensorvote3(T, out, *shape, sigma, 0.0, w, 1, 0, True, True, 20, True)
+    assert rel(u6(out), u6(ref)) < TOL
+    out2, _, _ = tv.vote3(T, sigma, 0.0, w=w, is_atv=True)
+    assert rel(u6(out2), u6(ref)) < TOL
+
+
 def test_vote3_sigma2_and_power3(tv):
     T = spd_field((9, 11, 12), 5)
     out, _, _ = tv.vote3(T, 2.0, 1.5, w=9, power=3, samples=7)

@@ -325,7 +325,7 @@ def vote3(field, sigma1, sigma2=0.0, w=0, power=1, samples=20, stick=True, plate
 
 def pipeline3(volume, sigma_st, sigma1, sigma2=0.0, w=0, power=1, samples=20, st_mode="same", stick=True,
               plate=True, ball=False, parity=True, out_layout="planes", out=True, evals=True, evecs="cartesian",
-              outputs=None):
+              outputs=None, is_atv=False):
     """Structure tensor -> vote -> fused eigendecomposition of a scalar
     volume (tvgb_pipeline3).  `outputs` may pass preallocated
     (out, evals, evecs) arrays (host or device).  Returns that triple."""
@@ -347,7 +347,7 @@ def pipeline3(volume, sigma_st, sigma1, sigma2=0.0, w=0, power=1, samples=20, st
             vec = _empty_like_kind(volume, dims + (6,))
     else:
         o, ev, vec = outputs
-    p = make_params(sigma1, sigma2, w, power, samples, stick, plate, ball, False, parity)
+    p = make_params(sigma1, sigma2, w, power, samples, stick, plate, ball, is_atv, parity)
     odims = (ctypes.c_uint * 3)()
     call("tvgb_pipeline3", _ptr(volume), s0, s1, s2, sigma_st, m, ctypes.byref(p), _ptr(o), OL, _ptr(ev), _ptr(vec),
          fmt, odims, _stream_for(volume, o, ev, vec))

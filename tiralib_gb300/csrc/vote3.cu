@@ -54,6 +54,7 @@ struct PrepOut {
     float* C;    // lambda0 (ball)
     float4* L;   // (lambda0, lambda1, lambda2, 0) -- ATV / generic
     float4* E1;  // middle eigenvector (ATV)
+    int atv;     // A, B, C hold the ATV scales: lambda2 - lambda1, lambda1 - lambda0, lambda0
 };
 
 template <int LAYOUT>
@@ -91,13 +92,15 @@ __global__ void __launch_bounds__(256) k_prep3(const float* __restrict__ in, siz
             eig3_precise_d(a, b, c, d, e, f, ev, v0, v1, v2);
         }
         if (o.A) {
-            const float ss = copysignf(fabsf(ev[2]) - fabsf(ev[1]), ev[2]);   // tensorvote.h:1537
-            o.A[i] = make_float4(v2[0], v2[1], v2[2], ss * sticknorm);
+            // TK: tensorvote.h:1537; ATV: atv_H's s1 = lambda2 - lambda1 (:660), no normaliser
+            const float ss = o.atv ? ev[2] - ev[1] : copysignf(fabsf(ev[2]) - fabsf(ev[1]), ev[2]) * sticknorm;
+            o.A[i] = make_float4(v2[0], v2[1], v2[2], ss);
         }
         if (o.B) {
             // plate3_numerical_device normalises the normal and skips a zero one (:2461-2465)
             const float nn = v0[0] * v0[0] + v0[1] * v0[1] + v0[2] * v0[2];
-            float sp = copysignf(fabsf(ev[1]) - fabsf(ev[0]), ev[1]);      // :2616
+            // TK: :2616; ATV: atv_H's s2 = lambda1 - lambda0 on the plane normal to n (:661)
+            float sp = o.atv ? ev[1] - ev[0] : copysignf(fabsf(ev[1]) - fabsf(ev[0]), ev[1]);
             float inv = 0.0f;
             if (nn > 1e-12f) inv = rsqrtf(nn); else sp = 0.0f;
             o.B[i] = make_float4(v0[0] * inv, v0[1] * inv, v0[2] * inv, sp);
@@ -127,6 +130,30 @@ __device__ __forceinline__ void radial_entry(int L2, float s1, float s2, float4&
                     ct * g * (2.0f / 15.0f));
 }
 
+// ATV (tensorvote.h:710) in the same closed-form terms.  With d the unit
+// offset (zero at the voter itself), R = I - 2 d d^T, c the attenuation
+// exp(-|o|^2 / sigma^2) and the voter's eigenpairs (l_k, e_k):
+//   stick  c (l2 - l1) (1 - (e2.d)^2) (R e2)(R e2)^T
+//   plate  c (l1 - l0) [(1 - |Pd|^2 / 4)(I - m m^T) - (R Pd)(R Pd)^T / 2],
+//          P = I - e0 e0^T = e1 e1^T + e2 e2^T, m = R e0, |Pd|^2 = 1 - (e0.d)^2
+//   ball   c l0 [(1 - |d|^2 / 5) I - (2 / 5) d d^T]
+// which is c R H R of atv_H (:607): for T = q q^T the H term reduces to
+// (1 - (q.d)^2) q q^T, R I R = I and R d = -d.  These are the basis tensors
+// the TK kernels accumulate (R q, I - m m^T, h = o + (n.o) m = -|o| R Pd,
+// and o o^T), so ATV runs on them with this radial table:
+//   a = (c, -c g, 2 g, A0),  b = (A1, Bp, ball I, ball oo^T),  g = 1 / |o|^2,
+//   A0 = c (3/4 for o != 0, 1 at o = 0), A1 = -c g / 4, Bp = -c g / 2,
+//   ball I = c (4/5 for o != 0, 1 at o = 0), ball oo^T = -2 c g / 5,
+// and voter records A = (e2, l2 - l1), B = (e0, l1 - l0), C = l0.
+__device__ __forceinline__ void radial_entry_atv(int L2, float sigma, float4& a, float4& b) {
+    const float l2 = float(L2);
+    const float c = sigma == 0.0f ? (l2 > 1e-12f ? 0.0f : 1.0f) : expf(-l2 / (sigma * sigma));   // atv_attenuation :35
+    const float g = L2 > 0 ? 1.0f / l2 : 0.0f;
+    const bool o0 = L2 == 0;
+    a = make_float4(c, -c * g, 2.0f * g, o0 ? c : 0.75f * c);
+    b = make_float4(-0.25f * c * g, -0.5f * c * g, o0 ? c : 0.8f * c, -0.4f * c * g);
+}
+
 // ------------------------------------------------------------------ fast kernel
 
 struct FastArgs {
@@ -142,7 +169,13 @@ struct FastArgs {
     int evec_fmt;
     int precise_eig;
     int zr0, zr1;               // receivers voted: planes [zr0, zr1) (launch_fast: [0, s0) if empty)
+    int atv;                    // ATV weights (radial_entry_atv, sigma = sig1) instead of TK's
 };
+
+__device__ __forceinline__ void fast_radial_entry(const FastArgs& a, int L2, float4& ea, float4& eb) {
+    if (a.atv) radial_entry_atv(L2, a.sig1, ea, eb);
+    else radial_entry(L2, a.sig1, a.sig2, ea, eb);
+}
 
 __device__ __forceinline__ void kahan_add(float& sum, float& comp, float x) {
     const float y = x - comp;
@@ -401,7 +434,7 @@ __global__ void __launch_bounds__(VX * VY, TVGB_FAST_MINB) k_vote3_fast(FastArgs
 
     for (int L2 = tid; L2 < nt; L2 += nthr) {
         float4 ea, eb;
-        radial_entry(L2, a.sig1, a.sig2, ea, eb);
+        fast_radial_entry(a, L2, ea, eb);
         tbl[2 * L2] = ea;
         tbl[2 * L2 + 1] = eb;
     }
@@ -674,7 +707,7 @@ __global__ void __launch_bounds__(VX * VY, TVGB_FAST_MINB) k_vote3_pk(FastArgs a
     const int nthr = VX * VY;
     for (int L2 = tid; L2 < nt; L2 += nthr) {
         float4 ea, eb;
-        radial_entry(L2, a.sig1, a.sig2, ea, eb);
+        fast_radial_entry(a, L2, ea, eb);
         tbl[2 * L2] = ea;
         tbl[2 * L2 + 1] = eb;
     }
@@ -1124,14 +1157,19 @@ int vote3_device(const float* in, int in_layout, unsigned s0, unsigned s1, unsig
     const bool S = !atv && p.stick, P = !atv && p.plate, B = !atv && p.ball;
     // exact plate whenever the rule has at least power + 2 points (or is the closed form)
     const bool plate_exact = p.samples == 0 || p.samples >= power + 2;
-    const bool fast = !atv && power == 1 && (!P || plate_exact);
+    // ATV runs on the fast kernel's stick, plate and ball terms with its own weights
+    // (radial_entry_atv) whenever the window's tables fit in shared memory
+    const bool atv_fast = atv && fast_smem(hw, 1, true, true, true) <= 200 * 1024;
+    const bool fast = atv_fast || (!atv && power == 1 && (!P || plate_exact));
+    const bool KS = S || atv_fast, KP = P || atv_fast, KB = B || atv_fast;   // terms of the fast kernel
 
     Scratch sA, sB, sC, sL, sE1, sGL;
     PrepOut po{};
-    if (S || atv) { TVGB_TRY(sA.alloc(n * 16, st)); po.A = sA.get<float4>(); }
-    if (P) { TVGB_TRY(sB.alloc(n * 16, st)); po.B = sB.get<float4>(); }
-    if (B) { TVGB_TRY(sC.alloc(n * 4, st)); po.C = sC.get<float>(); }
-    if (atv) {
+    po.atv = atv_fast ? 1 : 0;
+    if (KS || atv) { TVGB_TRY(sA.alloc(n * 16, st)); po.A = sA.get<float4>(); }
+    if (KP) { TVGB_TRY(sB.alloc(n * 16, st)); po.B = sB.get<float4>(); }
+    if (KB) { TVGB_TRY(sC.alloc(n * 4, st)); po.C = sC.get<float>(); }
+    if (atv && !atv_fast) {
         TVGB_TRY(sL.alloc(n * 16, st)); po.L = sL.get<float4>();
         TVGB_TRY(sE1.alloc(n * 16, st)); po.E1 = sE1.get<float4>();
     }
@@ -1144,18 +1182,19 @@ int vote3_device(const float* in, int in_layout, unsigned s0, unsigned s1, unsig
     fa.sig1 = p.sigma1; fa.sig2 = p.sigma2;
     fa.out = out; fa.out_layout = out_layout; fa.evals = evals3; fa.evecs = evecs; fa.evec_fmt = evec_format;
     fa.precise_eig = p.parity ? 0 : 1;
+    fa.atv = atv_fast ? 1 : 0;
     if (!S && !P && !B && !atv) {
         // nothing votes: the reference leaves the zeroed output
         if (out) TVGB_CUDA(cudaMemsetAsync(out, 0, n * (out_layout == TVGB_LAYOUT_MAT3 ? 36 : 24), st));
         if (!evals3 && !evecs) return TVGB_OK;
     }
     if (fast) {
-        if (!hook || hook->slab == 0) return launch_fast(fa, S, P, B, st);
+        if (!hook || hook->slab == 0) return launch_fast(fa, KS, KP, KB, st);
         // receivers in z-slabs of hook->slab planes; the hook follows each slab's launch
         for (unsigned z = 0; z < s0; z += hook->slab) {
             fa.zr0 = int(z);
             fa.zr1 = int(std::min(s0, z + hook->slab));
-            TVGB_TRY(launch_fast(fa, S, P, B, st));
+            TVGB_TRY(launch_fast(fa, KS, KP, KB, st));
             TVGB_TRY(hook->fn(hook->ctx, unsigned(fa.zr0), unsigned(fa.zr1)));
         }
         return TVGB_OK;
