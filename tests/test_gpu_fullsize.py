@@ -50,7 +50,7 @@ def six_to_mat(t6):
                     axis=1).reshape(-1, 3, 3)
 
 
-def check_eigenvectors(gvec, rvec, g6, r6, rev, label, c_solver=64.0):
+def check_eigenvectors(gvec, rvec, g6, r6, rev, label, c_solver=64.0, min_separated=0.05):
     """Eigenvectors up to sign against a reference decomposition, bounded by
     their conditioning.  For eigenvector k with eigenvalue gap g_k = min over
     j != k of |lambda_k - lambda_j| (reference eigenvalues), a perturbation E
@@ -62,10 +62,12 @@ def check_eigenvectors(gvec, rvec, g6, r6, rev, label, c_solver=64.0):
     the first term the two voted tensors' own difference, the second the
     FP32 closed-form solver's rounding.  Where that bound is below 1e-4 rad
     (well-separated eigenvalues), the benchmark spec's 1e-4 bar applies
-    directly, and at least 5% of the sample's e2 vectors must be in that
-    class so the check is not vacuous (in parity mode the two voted tensors
-    differ by ~2e-5 relative, FP32 summation order over 15 625 voters, so
-    only gaps above ~0.4 ||T|| qualify: 13% of the C2 sample's e2).
+    directly, and at least min_separated of the sample's e2 vectors must be
+    in that class so the check is not vacuous.  Against the reference's CPU
+    algorithm (parity mode) the two voted tensors differ by ~2e-5 relative
+    (FP32 summation order over 15 625 voters), so only gaps above ~0.4 ||T||
+    qualify (13% of the C2 sample's e2, none of C4's): there the bound
+    itself is the assertion, with min_separated = 0.
     Angles are atan2(|u x v|, |u . v|)
     of the normalised vectors (arccos of a dot product would turn the ~1e-7
     norm error of an FP32 vector into a spurious 3e-4 rad)."""
@@ -87,8 +89,10 @@ def check_eigenvectors(gvec, rvec, g6, r6, rev, label, c_solver=64.0):
                                 f"bound {bound[worst]:.3e} (gap/||T|| {gaps[worst] / Tn[worst[0]]:.3e}, "
                                 f"||dT||/||T|| {dT[worst[0]] / Tn[worst[0]]:.3e})")
     sep = bound < 1e-4
-    assert sep[:, 2].mean() >= 0.05, f"{label}: only {sep[:, 2].mean():.2f} of the e2 vectors are well separated"
-    assert ang[sep].max() < 1e-4, f"{label}: well-separated eigenvector turned {ang[sep].max():.3e} rad"
+    assert sep[:, 2].mean() >= min_separated, \
+        f"{label}: only {sep[:, 2].mean():.2f} of the e2 vectors are well separated"
+    if sep.any():
+        assert ang[sep].max() < 1e-4, f"{label}: well-separated eigenvector turned {ang[sep].max():.3e} rad"
     return float(ang[:, 2].max()), float(ang[:, 0].max())
 
 
@@ -146,7 +150,8 @@ def test_tube_field_at_full_size(torch_dev, name):
     cev = detail["evals"].astype(np.float64)
     assert (np.abs(gev - cev).max(1) / np.abs(cev).max(1)).max() < 1e-4
     # eigenvectors (eigen.h's evec3_symmetric on both sides, eigen.h:452) up to sign
-    check_eigenvectors(gvec, detail["evecs"].reshape(-1, 3, 3), g6, c6, cev, f"{name} parity vs reference CPU")
+    check_eigenvectors(gvec, detail["evecs"].reshape(-1, 3, 3), g6, c6, cev, f"{name} parity vs reference CPU",
+                       min_separated=0.0)
     del out, ev, vec
     # precise mode: the whole field's properties, and exact power-of-two scaling of the whole pipeline
     p1 = run3(tv, vol_d, cfg, parity=False)
