@@ -304,10 +304,11 @@ int tvgb_surrogate_eval_tc_limit(const float* params, const float* X, size_t n, 
                                  long long wait_limit, void* stream);
 
 /* tvgb_vote3 (TK, power 1, sigma2 = 0) with the plate (and ball) vote by
- * plate_mode: 0 the network (judged per CTA of 32 x 4 receivers: if any of
- * its first 32 receivers' plate differs from the exact plate by more than
- * tol x its voted tensor's norm, the CTA's plate is voted exactly), 1 the
- * exact closed form, 2 the plain 64-orientation integral.  The stick vote
+ * plate_mode: 0 the network (judged per CTA of 32 x 4 receivers: if its
+ * first 32 receivers' plate differs from the exact plate by more than tol x
+ * the norm of their voted tensors, normwise over the 32, the CTA's plate is
+ * voted exactly), 1 the exact closed form, 2 the plain 64-orientation
+ * integral.  The stick vote
  * is exact in every mode.  stats (2 values, host, may be NULL): CTAs, and
  * CTAs recomputed exactly. */
 int tvgb_vote3_surrogate(const float* in, int in_layout, unsigned s0, unsigned s1, unsigned s2,

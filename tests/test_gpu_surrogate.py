@@ -35,6 +35,10 @@ def test_samples_are_the_plain_integral(S):
     ref = np.array([O.surrogate_target(x[:3], x[3:6], int(x[6])) for x in X[:400]])
     np.testing.assert_allclose(T[:400, :6], ref, rtol=0, atol=2e-6)
     assert np.all(T[:, 6:] == 0) and np.all(X[:, 7] == 0)
+    # canonical inputs: plate n_z >= 0 and d.n >= 0; ball n = e_z and d_z >= 0
+    pl = X[:, 6] == 1.0
+    assert np.all(X[pl, 5] >= 0) and np.all((X[pl, :3] * X[pl, 3:6]).sum(1) >= -1e-7)
+    assert np.all(X[~pl, 3:6] == np.array([0, 0, 1], np.float32)) and np.all(X[~pl, 2] >= 0)
 
 
 def test_training_gradient_matches_fp64_mlp(S):

@@ -164,6 +164,7 @@ __global__ void k_sur_samples(size_t n, unsigned long long seed, float* __restri
         }
         float* xo = X + i * 8;
         float* to = T + i * 8;
+        sur_canonical(x, nv, plate);      // the target is the same at the canonical inputs
         xo[0] = x[0]; xo[1] = x[1]; xo[2] = x[2]; xo[3] = nv[0]; xo[4] = nv[1]; xo[5] = nv[2];
         xo[6] = plate ? 1.0f : 0.0f; xo[7] = 0.0f;
         for (int k = 0; k < 6; ++k) to[k] = F[k];

@@ -38,6 +38,23 @@ constexpr int SUR_NBIAS = 3 * SUR_H + SUR_OUT;   // b1 b2 b3 b4
 constexpr float GELU_K = 0.7978845608028654f;    // sqrt(2 / pi)
 constexpr float GELU_A = 0.044715f;
 
+// The network's inputs in canonical form.  The plate vote is even in the
+// offset direction d and in the normal n (R = I - 2 d d^T, m m^T and
+// (R p)(R p)^T with p = (I - n n^T) d are unchanged by either sign), and the
+// ball vote is even in d and does not depend on n.  So n is taken with
+// n_z >= 0 and d with d.n >= 0 (ball: d_z >= 0 and n = e_z): the network
+// learns each function on a quarter (plate) or half (ball) of its domain.
+// Training samples, the vote and the ball table all pass through here.
+__host__ __device__ __forceinline__ void sur_canonical(float* d, float* n, bool plate) {
+    if (plate) {
+        if (n[2] < 0.0f) { n[0] = -n[0]; n[1] = -n[1]; n[2] = -n[2]; }
+        if (d[0] * n[0] + d[1] * n[1] + d[2] * n[2] < 0.0f) { d[0] = -d[0]; d[1] = -d[1]; d[2] = -d[2]; }
+    } else {
+        n[0] = 0.0f; n[1] = 0.0f; n[2] = 1.0f;
+        if (d[2] < 0.0f) { d[0] = -d[0]; d[1] = -d[1]; d[2] = -d[2]; }
+    }
+}
+
 __device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
     const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);   // .x (low half) = lo
     return *reinterpret_cast<const uint32_t*>(&v);

@@ -1513,13 +1513,15 @@ extern "C" int tvgb_vote3_noalloc(const float* in, int in_layout, unsigned s0, u
 // vote by one of three rules, chosen so that they can be timed side by side
 // in the same kernel skeleton (one receiver per lane, 32 x 4 receivers per
 // CTA, voters read through L1 / L2):
-//   PLATE_SURROGATE  the MLP of surrogate_mlp.cuh on the tensor cores: for
-//                    each voter offset a warp runs its 32 (receiver, voter)
-//                    pairs as two 16-row tiles; o = 0 is voted exactly.  A
-//                    judge then votes the plate of the CTA's first 32
-//                    receivers exactly; if any of them differs from the
-//                    surrogate by more than tol x the norm of its full voted
-//                    tensor, the whole CTA's plate is recomputed exactly.
+//   PLATE_SURROGATE  the MLP of surrogate_mlp.cuh on the tensor cores
+//                    (sur_tc.cuh): for each voter offset the CTA runs its
+//                    128 (receiver, voter) pairs as one tile; o = 0 is voted
+//                    exactly.  A judge then votes the plate of the CTA's
+//                    first 32 receivers exactly; if the surrogate's plate
+//                    differs from it by more than tol x the norm of the full
+//                    voted tensors, normwise over those 32 receivers (the
+//                    tile's sampled error), the whole CTA's plate is
+//                    recomputed exactly.
 //   PLATE_CLOSED     the exact closed form of k_vote3_fast.
 //   PLATE_PLAIN64    the plain orientation integral with 64 orientations
 //                    (the reference's plate3_numerical_device rule,
@@ -1757,8 +1759,10 @@ __global__ void __launch_bounds__(128) k_vote3_surtc(SurVoteArgs a) {
                     vote_pair<false, true, false>(Z4, B, 0.0f, 0.0f, fmaf(B.x, oxf, B.y * oyf), oxf, oyf, ozf, ta, tb, P);
                 } else {
                     const float il = rsqrtf(float(L2));
-                    const uint32_t in8[8] = {pack_bf16x2(oxf * il, oyf * il), pack_bf16x2(ozf * il, B.x),
-                                             pack_bf16x2(B.y, B.z), pack_bf16x2(1.0f, 1.0f),
+                    float dv[3] = {oxf * il, oyf * il, ozf * il}, nv[3] = {B.x, B.y, B.z};
+                    sur_canonical(dv, nv, true);
+                    const uint32_t in8[8] = {pack_bf16x2(dv[0], dv[1]), pack_bf16x2(dv[2], nv[0]),
+                                             pack_bf16x2(nv[1], nv[2]), pack_bf16x2(1.0f, 1.0f),
                                              pack_bf16x2(1.0f, 0.0f), 0u, 0u, 0u};
                     if (!tcs.failed) tc::tmem_st8(tA, in8);
                     if (!sur_tc_layer<1>(tcs)) { ok = false; break; }
@@ -1809,15 +1813,21 @@ __global__ void __launch_bounds__(128) k_vote3_surtc(SurVoteArgs a) {
         float E[7];
         plate_exact_sum<BALL>(a, tbl, x, y, z, E);
         const float e6[6] = {E[0] + E[6], E[1], E[2], E[3] + E[6], E[4], E[5] + E[6]};
+        // the tile's sampled error, normwise over its 32 sampled receivers (Frobenius norms, off-diagonal
+        // entries twice): || plate_net - plate_exact || against tol x || voted tensor ||
         float dn = 0.0f, tn = 0.0f;
-        for (int k = 0; k < 6; ++k) {
-            const float wgt = (k == 0 || k == 3 || k == 5) ? 1.0f : 2.0f;
-            const float d = plate[k] - e6[k], tt = tot[k] + e6[k];
-            dn = fmaf(wgt * d, d, dn);
-            tn = fmaf(wgt * tt, tt, tn);
+        if (mine)
+            for (int k = 0; k < 6; ++k) {
+                const float wgt = (k == 0 || k == 3 || k == 5) ? 1.0f : 2.0f;
+                const float d = plate[k] - e6[k], tt = tot[k] + e6[k];
+                dn = fmaf(wgt * d, d, dn);
+                tn = fmaf(wgt * tt, tt, tn);
+            }
+        for (int off = 16; off > 0; off >>= 1) {
+            dn += __shfl_xor_sync(0xffffffffu, dn, off);
+            tn += __shfl_xor_sync(0xffffffffu, tn, off);
         }
-        const bool bad = mine && !(dn <= a.tol * a.tol * tn);
-        if (__any_sync(0xffffffffu, bad) && lane == 0) s_fail = 1;
+        if (lane == 0 && !(dn <= a.tol * a.tol * tn)) s_fail = 1;
     }
     __syncthreads();
     if (s_fail) {
@@ -1996,8 +2006,10 @@ extern "C" int tvgb_vote3_surrogate(const float* in, int in_layout, unsigned s0,
                 const int ox = int(i % W) - hw, oy = int((i / W) % W) - hw, oz = int(i / (size_t(W) * W)) - hw;
                 const int L2 = ox * ox + oy * oy + oz * oz;
                 const float il = L2 ? 1.0f / std::sqrt(float(L2)) : 0.0f;   // o = 0 is tabulated exactly
-                X[i * 8 + 0] = ox * il; X[i * 8 + 1] = oy * il; X[i * 8 + 2] = oz * il;
-                X[i * 8 + 5] = 1.0f;   // any unit normal: the ball does not depend on it
+                float dv[3] = {ox * il, oy * il, oz * il}, nv[3];
+                sur_canonical(dv, nv, false);       // the ball does not depend on the normal
+                X[i * 8 + 0] = dv[0]; X[i * 8 + 1] = dv[1]; X[i * 8 + 2] = dv[2];
+                X[i * 8 + 3] = nv[0]; X[i * 8 + 4] = nv[1]; X[i * 8 + 5] = nv[2];
             }
             TVGB_TRY(sX.alloc(nt3 * 32, st));
             TVGB_TRY(sY.alloc(nt3 * 32, st));

@@ -136,8 +136,9 @@ def evaluate(params, X, engine="tcgen05", gelu="bf16", wait_limit=None):
 def vote3(field, sigma, params=None, mode="surrogate", tol=1e-3, w=0, stick=True, plate=True, ball=False,
           parity=True, layout="mat3", out_layout="mat3", evals=False, evecs=None):
     """3D TK vote (power 1, sigma2 = 0) with the plate / ball vote by `mode`:
-    "surrogate" (the network, judged per CTA against the exact plate with
-    tolerance tol), "closed" (exact closed form) or "plain64" (the plain
+    "surrogate" (the network, judged per CTA against the exact plate of 32
+    of its receivers, normwise, with tolerance tol), "closed" (exact closed
+    form) or "plain64" (the plain
     64-orientation integral).  Returns (voted field, evals, evecs, stats)
     with stats = (CTAs, CTAs recomputed exactly)."""
     field = _api._check_f32(field, "field")
