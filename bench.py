@@ -320,10 +320,11 @@ def run_reference(args, rank):
         times.append(t)
     total = float(np.sum(times))
     value = args.steps * nrec / total
+    algo = ("ATV (tira::cpu::tensorvote3_atv's algorithm, tensorvote.h:710)" if cfg["atv"] else
+            f"stick + {cfg['samples']}-sample plate (tira::cpu::tensorvote3's algorithm"
+            f"{'; the reference has no TK ball' if cfg['ball'] else ''})")
     sample = (f"{args.ref_block}^3 interior receivers (+{cfg['w'] // 2}-voxel window halo) of the {cfg['n']}^3 "
-              f"volume per step: structure tensor, stick + {cfg['samples']}-sample plate (tira::cpu::tensorvote3's "
-              f"algorithm{'; the reference has no TK ball' if cfg['ball'] else ''}), 3x3 eigen of the voted tensors; "
-              f"OpenMP over receivers")
+              f"volume per step: structure tensor, {algo}, 3x3 eigen of the voted tensors; OpenMP over receivers")
     line = {
         "impl": "reference", "metric": metric_for(cfg), "value": value, "unit": "voxels/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
@@ -560,17 +561,40 @@ def run_ours(args, rank, world, local_rank):
             "metric": metric_for(cfg), "value": value, "unit": "voxels/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
             "scaling": "strong" if strong else "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": dict(config_dict(cfg), parallelism=(f"z-slabs x{world} (halo planes, no collective)" if strong
-                                                          else f"replicas x{world}")),
+            "config": config_dict(cfg),
+            "parallelism": (f"z-slabs x{world} (halo planes, no collective)" if strong else f"replicas x{world}"),
             "e2e": {"value": e2e_value, "unit": "voxels/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
             "kernels": {k: {"launches": v[0], "total_ms": v[1]} for k, v in prof.items()},
             "memory": memory, "surrogate": sur, "accuracy": accuracy,
         }
+        if world == 1 and not args.no_secondary and not strong:
+            line["secondary"] = secondary_configs(args, local_rank)
         print(json.dumps(line), flush=True)
     if dist:
         dist.barrier()
         dist.destroy_process_group()
+
+
+def secondary_configs(args, local_rank):
+    """Compact measurements of the other workloads, after the headline's: C1
+    (the 2D path, 512^2: value, e2e, FP32 roofline of the vote) and C3 (2^27
+    tensors in precise mode: value, HBM roofline of the eigensolver; no host
+    round trip).  A few seconds of GPU time."""
+    out = {}
+    a1 = argparse.Namespace(**vars(args))
+    a1.config, a1.size, a1.steps, a1.warmup, a1.no_cpu_baseline = "c1", 0, 5, 3, True
+    l1 = run_c1(a1, 0, 1, local_rank, emit=False)
+    out["c1"] = {"workload": l1["config"]["workload"], "metric": l1["metric"], "value": l1["value"],
+                 "unit": l1["unit"], "ms_per_step": l1["ms_per_step"], "e2e": l1["e2e"], "roofline": l1["roofline"],
+                 "clocks": l1["clocks"]}
+    a3 = argparse.Namespace(**vars(args))
+    a3.config, a3.size, a3.steps, a3.warmup, a3.no_cpu_baseline = "c3", 0, 3, 3, True
+    l3 = run_c3(a3, 0, 1, local_rank, emit=False, light=True)
+    out["c3"] = {"workload": l3["config"]["workload"], "metric": l3["metric"], "value": l3["value"],
+                 "unit": l3["unit"], "ms_per_step": l3["ms_per_step"], "roofline": l3["roofline"],
+                 "fp64_refined_fraction": l3["fp64_refined_fraction"], "clocks": l3["clocks"]}
+    return out
 
 
 # ----------------------------------------------------------------------------- surrogate vs plain
@@ -724,7 +748,7 @@ def eigen_errors(m9, ev, vec):
             "backward": stat(bw), "n": int(len(m9))}
 
 
-def run_c3(args, rank, world, local_rank):
+def run_c3(args, rank, world, local_rank, emit=True, light=False):
     import torch
     import tiralib_gb300 as tv
     torch.cuda.set_device(local_rank)
@@ -765,25 +789,27 @@ def run_c3(args, rank, world, local_rank):
     with ClockSampler(gpu_index_for(local_rank)) as clk:
         t_precise, launches, prof = timed(True)
     clocks = clk.summary()
-    ev_p, vec_p = ev[idx].cpu().numpy(), vec[idx].cpu().numpy()
-    t_parity, _, prof_par = timed(False)
-    ev_r, vec_r = ev[idx].cpu().numpy(), vec[idx].cpu().numpy()
     _, _, nref = tv.eig3(mats[: 1 << 20], precise=True)
-    m_h = mats[idx].cpu().numpy()
-    err_precise = eigen_errors(m_h, ev_p, vec_p)
-    err_parity = eigen_errors(m_h, ev_r, vec_r)
-    # end to end with pinned host buffers
-    mats_h = mats.cpu().pin_memory()
-    ev_h = torch.empty((n, 3)).pin_memory()
-    vec_h = torch.empty((n, 3, 3)).pin_memory()
-    mn, evn, vecn = mats_h.numpy(), ev_h.numpy(), vec_h.numpy()
-    # one full-size untimed call: the library's memory pool grows to the chunk ring's size once
-    tv.api.call("tvgb_eig3", tv.api._ptr(mn), 9, n, tv.api._ptr(evn), tv.api._ptr(vecn), 1, 1, None, None)
-    e2e = []
-    for _ in range(max(1, min(args.steps, 3))):
-        t0 = time.perf_counter()
+    t_parity, err_precise, err_parity, e2e = None, None, None, None
+    if not light:
+        ev_p, vec_p = ev[idx].cpu().numpy(), vec[idx].cpu().numpy()
+        t_parity, _, prof_par = timed(False)
+        ev_r, vec_r = ev[idx].cpu().numpy(), vec[idx].cpu().numpy()
+        m_h = mats[idx].cpu().numpy()
+        err_precise = eigen_errors(m_h, ev_p, vec_p)
+        err_parity = eigen_errors(m_h, ev_r, vec_r)
+        # end to end with pinned host buffers
+        mats_h = mats.cpu().pin_memory()
+        ev_h = torch.empty((n, 3)).pin_memory()
+        vec_h = torch.empty((n, 3, 3)).pin_memory()
+        mn, evn, vecn = mats_h.numpy(), ev_h.numpy(), vec_h.numpy()
+        # one full-size untimed call: the library's memory pool grows to the chunk ring's size once
         tv.api.call("tvgb_eig3", tv.api._ptr(mn), 9, n, tv.api._ptr(evn), tv.api._ptr(vecn), 1, 1, None, None)
-        e2e.append(time.perf_counter() - t0)
+        e2e = []
+        for _ in range(max(1, min(args.steps, 3))):
+            t0 = time.perf_counter()
+            tv.api.call("tvgb_eig3", tv.api._ptr(mn), 9, n, tv.api._ptr(evn), tv.api._ptr(vecn), 1, 1, None, None)
+            e2e.append(time.perf_counter() - t0)
     peaks = measured_peaks()
     # the precise call is one k_eig3 launch (FP32 solve, FP64 refinement of the flagged tensors from the tile
     # in shared memory): its roofline is the call's algorithmic bytes over the kernel's time per call
@@ -801,8 +827,9 @@ def run_c3(args, rank, world, local_rank):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         v, th, desc = cpu_eigen_sample()
         cpu = {"value": v, "unit": "tensors/s", "cores": th, "kind": "port", "sample": desc}
+    line = None
     if rank == 0:
-        print(json.dumps({
+        line = {
             "metric": C3_METRIC, "value": world * args.steps * n / t_precise, "unit": "tensors/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_precise / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 refinement)",
@@ -811,14 +838,19 @@ def run_c3(args, rank, world, local_rank):
                                    " 10% near-degenerate pair, 1% fully degenerate; mat3 in, eigenvalues + "
                                    "cartesian eigenvectors out", "tensors": n,
                        "l2_flush": "256 MiB write between timed steps (outside the events)"},
-            "parity_mode_tensors_per_s": args.steps * n / t_parity,
+            "parity_mode_tensors_per_s": args.steps * n / t_parity if t_parity else None,
             "fp64_refined_fraction": nref / float(1 << 20),
             "errors_vs_fp64": {"precise": err_precise, "parity": err_parity},
-            "e2e": {"value": n / float(np.mean(e2e)), "unit": "tensors/s", "h2d_bytes_per_step": n * 36,
-                    "d2h_bytes_per_step": n * 48},
+            "e2e": ({"value": n / float(np.mean(e2e)), "unit": "tensors/s", "h2d_bytes_per_step": n * 36,
+                     "d2h_bytes_per_step": n * 48} if e2e else None),
             "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cpu, "clocks": clocks,
             "kernels": {k: {"launches": v[0], "total_ms": v[1]} for k, v in prof.items()},
-        }), flush=True)
+        }
+        if emit:
+            print(json.dumps(line), flush=True)
+    del mats, ev, vec
+    torch.cuda.empty_cache()
+    return line
 
 
 def cpu_eigen_sample(n=1 << 20):
@@ -870,7 +902,7 @@ def run_c3_reference(args, rank):
 C1_METRIC = "2D tensor-vote pixels/s (structure tensor sigma 1 -> stick+plate vote sigma 3 -> 2x2 eigen)"
 
 
-def run_c1(args, rank, world, local_rank):
+def run_c1(args, rank, world, local_rank, emit=True):
     import torch
     import tiralib_gb300 as tv
     from tiralib_gb300 import workloads as W
@@ -985,8 +1017,9 @@ def run_c1(args, rank, world, local_rank):
         cpu = {"value": crop.size / tc, "unit": "pixels/s", "cores": 1, "kind": "port",
                "sample": "192x192 crop: the reference's CPU 2D path (tira::cpu::tensorvote's algorithm, single "
                          "thread as shipped) incl. structure tensor and eigenpairs"}
+    line = None
     if rank == 0:
-        print(json.dumps({
+        line = {
             "metric": C1_METRIC, "value": world * args.steps * n / t, "unit": "pixels/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -1001,7 +1034,10 @@ def run_c1(args, rank, world, local_rank):
             "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cpu, "clocks": clk.summary(),
             "kernels": {k: {"launches": v[0], "total_ms": v[1]} for k, v in prof.items()},
             "memory": memory,
-        }), flush=True)
+        }
+        if emit:
+            print(json.dumps(line), flush=True)
+    return line
 
 
 def run_c1_reference(args, rank):
@@ -1051,6 +1087,7 @@ def main():
     ap.add_argument("--ref-block", type=int, default=12, help="edge of the CPU reference's receiver block")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-surrogate", action="store_true", help="skip the surrogate-vs-plain study")
+    ap.add_argument("--no-secondary", action="store_true", help="skip the C1 / C3 measurements after the headline")
     ap.add_argument("--sur-block", type=int, default=128, help="edge of the surrogate study's interior block")
     ap.add_argument("--sur-reps", type=int, default=1, help="timed launches per mode of the surrogate study")
     ap.add_argument("--sur-warm", type=int, default=1, help="1: one untimed launch per mode first")
