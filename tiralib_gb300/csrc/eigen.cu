@@ -33,7 +33,7 @@ constexpr int EIG_BLOCK = 256;
 // resident blocks per SM the precise kernel is compiled for: its FP64 phase
 // would otherwise take the register count past 64 per thread
 #ifndef TVGB_EIG_MINB
-#define TVGB_EIG_MINB 4
+#define TVGB_EIG_MINB 5
 #endif
 
 // in_layout: 9 (mat3 AoS), 6 (sym6 AoS), 60 (sym6 planes)
