@@ -532,6 +532,18 @@ def run_ours(args, rank, world, local_rank):
                     "flops_per_launch": flops, "flops_per_pair": per_pair, "avg_launch_ms": avg_s * 1e3,
                     "share_of_step": (tot_ms / (np.sum(times))) if np.sum(times) else None}
 
+    # the structure tensor's kernel against the HBM roofline: 4 B in + 24 B out per voxel
+    st_roof = None
+    st_name = "k_st3_tma" if "k_st3_tma" in prof else "k_st3"
+    nl_st, tot_st = prof.get(st_name, (0, 0.0))
+    if nl_st:
+        avg_st = tot_st / nl_st / 1e3
+        hbm = measured_peaks()
+        st_ach = nvox * 28 / avg_st / 1e9
+        st_roof = {"bound": "hbm", "kernel": st_name, "achieved": st_ach, "peak": hbm["hbm_gbs"], "unit": "GB/s",
+                   "frac": st_ach / hbm["hbm_gbs"], "peak_source": hbm["source"], "bytes_per_voxel": 28,
+                   "avg_launch_ms": avg_st * 1e3}
+
     sur = None
     if rank == 0 and world == 1 and not args.no_surrogate and not strong and not cfg["atv"]:
         sur = surrogate_study(vol_d, cfg, args, dev)
@@ -567,6 +579,7 @@ def run_ours(args, rank, world, local_rank):
             "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
             "kernels": {k: {"launches": v[0], "total_ms": v[1]} for k, v in prof.items()},
             "memory": memory, "surrogate": sur, "accuracy": accuracy,
+            "structure_tensor_roofline": st_roof,
         }
         if world == 1 and not args.no_secondary and not strong:
             line["secondary"] = secondary_configs(args, local_rank)

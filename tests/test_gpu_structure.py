@@ -90,3 +90,54 @@ def test_pipeline3_matches_chained_oracle(tv):
     assert rel(out.reshape(-1, 9)[:, u], ref.reshape(-1, 9)[:, u]) < 1e-4
     ref_ev = O.evals3(out.reshape(-1, 9))
     assert (np.abs(ev.reshape(-1, 3) - ref_ev).max(axis=1) / np.abs(ref_ev).max(axis=1)).max() < 1e-5
+
+
+def _profiled(tv, fn):
+    """Run fn with the library's kernel timing on; the kernel names that ran."""
+    import ctypes
+    L = tv.lib()
+    buf = ctypes.create_string_buffer(1 << 14)
+    L.tvgb_profile_enable(1)
+    L.tvgb_profile_read(buf, len(buf))
+    out = fn()
+    L.tvgb_profile_read(buf, len(buf))
+    L.tvgb_profile_enable(0)
+    return out, {line.split()[0] for line in buf.value.decode().strip().splitlines() if line.strip()}
+
+
+@pytest.mark.parametrize("mode", ["valid", "same"])
+@pytest.mark.parametrize("sigma", [0.3, 0.7, 1.0, 1.5, 1.7, 2.0])      # 3, 5, 7, 9, 11, 13 taps
+@pytest.mark.parametrize("shape", [(21, 22, 24), (9, 70, 64), (40, 17, 36), (6, 8, 32)])
+def test_structure_tensor3_tma_kernel_matches_oracle(tv, mode, sigma, shape):
+    """Volumes whose rows are 16-byte multiples (s2 % 4 == 0) take the
+    TMA-staged kernel (k_st3_tma): every tap count of the fixed-tap
+    kernels, both output modes, faces in every axis, several CTAs in x and
+    y, fewer planes than taps; against the oracle's restatement of
+    volume::gradient + the separable Gaussian (filter.h)."""
+    K = int(np.ceil(6 * sigma)) | 1
+    if mode == "valid" and min(shape) < K:
+        pytest.skip("valid output empty: the volume is smaller than the window")
+    rng = np.random.default_rng(sum(shape) + int(10 * sigma))
+    v = rng.normal(size=shape).astype(np.float32)
+    out, ran = _profiled(tv, lambda: tv.structure_tensor3(v, sigma, mode=mode, layout="planes"))
+    assert "k_st3_tma" in ran
+    ref = O.structure_tensor3(v, sigma, 0 if mode == "valid" else 1)
+    assert out.shape == ref.shape
+    assert rel(out, ref) < 1e-5
+
+
+def test_structure_tensor3_tma_kernel_layouts(tv):
+    """The TMA kernel's three output layouts hold the same numbers, and the
+    rows that are not 16-byte multiples take the other kernel."""
+    rng = np.random.default_rng(3)
+    v = rng.normal(size=(13, 19, 28)).astype(np.float32)
+    (p, ran) = _profiled(tv, lambda: tv.structure_tensor3(v, 1.5, layout="planes"))
+    assert "k_st3_tma" in ran
+    s6 = tv.structure_tensor3(v, 1.5, layout="sym6")
+    m = tv.structure_tensor3(v, 1.5, layout="mat3")
+    np.testing.assert_array_equal(np.moveaxis(p, 0, -1), s6)
+    m9 = m.reshape(-1, 9)
+    np.testing.assert_array_equal(m9[:, [0, 1, 2, 4, 5, 8]], s6.reshape(-1, 6))
+    np.testing.assert_array_equal(m9[:, [3, 6, 7]], m9[:, [1, 2, 5]])
+    _, ran = _profiled(tv, lambda: tv.structure_tensor3(v[:, :, :27].copy(), 1.5))
+    assert "k_st3_tma" not in ran and "k_st3" in ran

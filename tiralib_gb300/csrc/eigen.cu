@@ -188,6 +188,169 @@ __global__ void __launch_bounds__(EIG_BLOCK, PRECISE ? TVGB_EIG_MINB : 1) k_eig3
     if (PRECISE && n_refined && threadIdx.x == 0 && refined) atomicAdd(n_refined, (unsigned long long)refined);
 }
 
+// Precise mode, warp-tiled.  Each warp owns tiles of 32 consecutive tensors
+// (tile t of the batch goes to warp t mod (warps in the grid)) and works on
+// them without any block-wide barrier:
+//   * the next tile's records are copied into the warp's shared buffer with
+//     cp.async while the current one is solved;
+//   * every lane solves its tensor in FP32 (eig3_precise_fp32); a tensor
+//     whose remaining pair is closer than 1e-4 |lambda_max| is appended to
+//     the warp's queue in shared memory (its six entries, w and its place);
+//   * the tile's results leave through the warp's staging buffer with
+//     16-byte coalesced stores;
+//   * once the queue holds 32 tensors, the warp finishes them in FP64, one
+//     per lane, and writes their results over the FP32 ones (the tiles they
+//     came from were stored a few tiles earlier and are normally still in
+//     L2).  The rest of the queue is finished at the end.
+// A warp busy in FP64 holds up no other warp, so the FP64 pipe works while
+// the other warps issue the FP32 phase.
+constexpr int EIGW_QCAP = 64;          // queue entries per warp (at most 31 + 32 between drains)
+constexpr int EIGW_QF = 11;            // floats per entry: 6 entries, w0..w2, tile, key
+
+template <int IN_LAYOUT, int EVEC_FMT>
+__global__ void __launch_bounds__(EIG_BLOCK, TVGB_EIG_MINB) k_eig3w(const float* __restrict__ in, size_t n,
+                                                                      float* __restrict__ evals,
+                                                                      float* __restrict__ evecs,
+                                                                      unsigned long long* __restrict__ n_refined,
+                                                                      int aligned_in, int aligned_out) {
+    constexpr int NF = IN_LAYOUT == 9 ? 9 : 6;
+    constexpr int NV = EVEC_FMT == 1 ? 9 : (EVEC_FMT == 2 ? 6 : 0);
+    constexpr int NW = EIG_BLOCK / 32;
+    __shared__ __align__(16) float s_in[NW][32 * NF];
+    __shared__ __align__(16) float s_ev[NW][32 * 3];
+    __shared__ __align__(16) float s_vec[NW][32 * (NV ? NV : 1)];
+    __shared__ float s_q[NW][EIGW_QCAP * EIGW_QF];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const size_t nwarps = size_t(gridDim.x) * NW;
+    const size_t ntiles = (n + 31) / 32;
+    float* sin = s_in[warp];
+    float* sq = s_q[warp];
+    int qn = 0;                         // warp-uniform queue length
+    unsigned long long refined = 0;
+
+    // the tile's AoS records into the warp buffer: asynchronous when whole and aligned
+    auto fetch = [&](size_t t) {
+        if (IN_LAYOUT == 60) return;
+        const size_t base = t * 32;
+        const int cnt = int(min(size_t(32), n - base));
+        const float* src = in + base * NF;
+        if (aligned_in && cnt == 32) {
+            const uint32_t dst = static_cast<uint32_t>(__cvta_generic_to_shared(sin));
+            for (int i = lane; i < 32 * NF / 4; i += 32)
+                asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst + 16u * i), "l"(src + 4 * i)
+                             : "memory");
+            asm volatile("cp.async.commit_group;" ::: "memory");
+        } else {
+            for (int i = lane; i < cnt * NF; i += 32) sin[i] = __ldg(src + i);
+        }
+    };
+    // FP64 phase of queue entries [q0, q0 + cnt) (one per lane), results written to global memory
+    auto drain = [&](int q0, int cnt) {
+        if (lane < cnt) {
+            const float* e = sq + (q0 + lane) * EIGW_QF;
+            const unsigned key = __float_as_uint(e[10]);
+            const size_t i = size_t(__float_as_uint(e[9])) * 32 + (key & 31u);
+            const int code = int((key >> 5) & 3u);
+            const bool hi = (key >> 7) & 1u;
+            const float w[3] = {e[6], e[7], e[8]};
+            float ev[3], v[9];
+            eig3_precise_fp64(e[0], e[1], e[2], e[3], e[4], e[5], w, hi, code, ev, v, v + 3, v + 6);
+            if (evals) { evals[i * 3] = ev[0]; evals[i * 3 + 1] = ev[1]; evals[i * 3 + 2] = ev[2]; }
+            if (EVEC_FMT == 1 && evecs)
+                for (int k = 0; k < 9; ++k) evecs[i * 9 + k] = v[k];
+            if (EVEC_FMT == 2 && evecs) {
+                float th, ph;
+                to_spherical_d(v, th, ph); evecs[i * 6] = th; evecs[i * 6 + 1] = ph;
+                to_spherical_d(v + 3, th, ph); evecs[i * 6 + 2] = th; evecs[i * 6 + 3] = ph;
+                to_spherical_d(v + 6, th, ph); evecs[i * 6 + 4] = th; evecs[i * 6 + 5] = ph;
+            }
+        }
+        refined += unsigned(cnt);
+    };
+
+    size_t t = blockIdx.x * size_t(NW) + warp;
+    if (t < ntiles) fetch(t);
+    for (; t < ntiles; t += nwarps) {
+        const size_t base = t * 32;
+        const int cnt = int(min(size_t(32), n - base));
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
+        __syncwarp();
+        float a = 0, b = 0, c = 0, d = 0, e = 0, f = 0;
+        if (lane < cnt) {
+            if (IN_LAYOUT == 60) {
+                const size_t i = base + lane;
+                a = __ldg(in + i); b = __ldg(in + n + i); d = __ldg(in + 2 * n + i);
+                c = __ldg(in + 3 * n + i); e = __ldg(in + 4 * n + i); f = __ldg(in + 5 * n + i);
+            } else if (NF == 9) {
+                const float* m = sin + lane * 9;
+                a = m[0]; b = m[1]; d = m[2]; c = m[4]; e = m[5]; f = m[8];
+            } else {
+                const float* m = sin + lane * 6;
+                a = m[0]; b = m[1]; d = m[2]; c = m[3]; e = m[4]; f = m[5];
+            }
+        }
+        __syncwarp();                                       // the buffer is read: the next copy may land
+        if (t + nwarps < ntiles) fetch(t + nwarps);
+        float ev[3] = {0, 0, 0}, v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, w[3];
+        bool hi = true;
+        int code = 0;
+        if (lane < cnt) code = eig3_precise_fp32(a, b, c, d, e, f, ev, v, v + 3, v + 6, w, hi);
+        const unsigned flag = __ballot_sync(0xffffffffu, code != 0);
+        if (code) {   // queue slot: after the lanes below with a flagged tensor
+            float* q = sq + (qn + __popc(flag & ((1u << lane) - 1u))) * EIGW_QF;
+            q[0] = a; q[1] = b; q[2] = c; q[3] = d; q[4] = e; q[5] = f;
+            q[6] = w[0]; q[7] = w[1]; q[8] = w[2];
+            q[9] = __uint_as_float(unsigned(t));
+            q[10] = __uint_as_float(unsigned(lane) | (unsigned(code) << 5) | ((hi ? 1u : 0u) << 7));
+        }
+        qn += __popc(flag);
+        // the tile's FP32 results (flagged tensors: overwritten by their FP64 phase later)
+        float* se = s_ev[warp];
+        se[lane * 3] = ev[0]; se[lane * 3 + 1] = ev[1]; se[lane * 3 + 2] = ev[2];
+        if (NV) {
+            float* sv = s_vec[warp];
+            if (EVEC_FMT == 1) {
+                for (int k = 0; k < 9; ++k) sv[lane * 9 + k] = v[k];
+            } else {
+                float sph[6];
+                to_spherical_d(v, sph[0], sph[1]);
+                to_spherical_d(v + 3, sph[2], sph[3]);
+                to_spherical_d(v + 6, sph[4], sph[5]);
+                for (int k = 0; k < 6; ++k) sv[lane * 6 + k] = sph[k];
+            }
+        }
+        __syncwarp();
+        const bool full = cnt == 32 && aligned_out;
+        if (evals) {
+            if (full) {
+                const float4* s4 = reinterpret_cast<const float4*>(se);
+                float4* d4 = reinterpret_cast<float4*>(evals + base * 3);
+                for (int i = lane; i < 24; i += 32) d4[i] = s4[i];
+            } else {
+                for (int i = lane; i < cnt * 3; i += 32) evals[base * 3 + i] = se[i];
+            }
+        }
+        if (NV && evecs) {
+            const float* sv = s_vec[warp];
+            if (full) {
+                const float4* s4 = reinterpret_cast<const float4*>(sv);
+                float4* d4 = reinterpret_cast<float4*>(evecs + base * NV);
+                for (int i = lane; i < 8 * NV; i += 32) d4[i] = s4[i];
+            } else {
+                for (int i = lane; i < cnt * NV; i += 32) evecs[base * NV + i] = sv[i];
+            }
+        }
+        __syncwarp();                                       // tile stores ordered before the FP64 results
+        if (qn >= 32) {
+            drain(qn - 32, 32);
+            qn -= 32;
+            __syncwarp();
+        }
+    }
+    if (qn > 0) drain(0, qn);
+    if (n_refined && lane == 0 && refined) atomicAdd(n_refined, refined);
+}
+
 __global__ void k_eval2(const float4* __restrict__ m4, size_t n, float2* __restrict__ ev2) {
     for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x) {
         const float4 m = __ldg(m4 + i);
@@ -257,6 +420,14 @@ static int launch_eig3_t(const float* in, size_t n, const float* ev_in, float* e
                          cudaStream_t s) {
     const int ai = (reinterpret_cast<uintptr_t>(in) % 16) == 0;
     const int ao = (!ev || reinterpret_cast<uintptr_t>(ev) % 16 == 0) && (!vec || reinterpret_cast<uintptr_t>(vec) % 16 == 0);
+    if (PR && !EI) {   // precise: the warp-tiled kernel
+        KernelTimer kt_("k_eig3", s);
+        k_eig3w<IL, EF><<<resident_grid(k_eig3w<IL, EF>, EIG_BLOCK, n), EIG_BLOCK, 0, s>>>(in, n, ev, vec, nref, ai,
+                                                                                            ao);
+        kt_.stop();
+        TVGB_LAUNCHED();
+        return TVGB_OK;
+    }
     {
         KernelTimer kt_("k_eig3", s);
         k_eig3<IL, EF, PR, EI><<<resident_grid(k_eig3<IL, EF, PR, EI>, EIG_BLOCK, n), EIG_BLOCK, 0, s>>>(

@@ -1,6 +1,8 @@
 // Host-side support of libtvgb: error state, pointer classification and
 // stream-ordered device temporaries.
 #include "tvgb_common.cuh"
+#include "tma_sm100.cuh"
+#include <cudaTypedefs.h>
 #include <map>
 #include <mutex>
 #include <string>
@@ -210,6 +212,38 @@ __global__ void __launch_bounds__(256) k_tanh_rate(int iters, float* __restrict_
 #pragma unroll
     for (int i = 0; i < 8; ++i) s += a[i] + __uint_as_float(b[i]);
     if (s == 1234.5f) sink[0] = s;
+}
+
+// ------------------------------------------------------------------ TMA tensor maps
+// cuTensorMapEncodeTiled is a driver API function; the library links only the
+// runtime, so its address is looked up once through the runtime.
+bool make_tmap_3d_f32(CUtensorMap* map, const float* base, unsigned s2, unsigned s1, unsigned s0, unsigned bx,
+                      unsigned by) {
+    static std::once_flag once;
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    std::call_once(once, [] {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+        else
+            cudaGetLastError();
+    });
+    if (!encode) return false;
+    if (reinterpret_cast<uintptr_t>(base) % 16 != 0 || (size_t(s2) * 4) % 16 != 0 || (bx * 4) % 16 != 0) return false;
+    const cuuint64_t dims[3] = {s2, s1, s0};
+    const cuuint64_t strides[2] = {cuuint64_t(s2) * 4, cuuint64_t(s2) * s1 * 4};
+    const cuuint32_t box[3] = {bx, by, 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    CUtensorMap m;
+    const CUresult r = encode(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), dims, strides, box, estr,
+                              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                              CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return false;
+    *map = m;
+    return true;
 }
 
 }  // namespace tvgb
