@@ -7,9 +7,12 @@
  * Parameter layout (float64 here, float32 master copy on the GPU), padded to
  * 8 inputs / 8 outputs with zero rows / columns:
  *   W1[64][8] b1[64] W2[64][64] b2[64] W3[64][64] b3[64] W4[8][64] b4[8]
- * Quantised forward (quant != 0): weights and each layer's input rounded to
- * bfloat16 (round to nearest even of the float32 value), as the tensor-core
- * inference computes; the backward pass treats the rounding as identity.
+ * Quantised forward (quant != 0): weights and each hidden layer's input
+ * rounded to bfloat16 (round to nearest even of the float32 value), the
+ * network's inputs taken as bf16(x) + bf16(x - bf16(x)) (the tensor-core
+ * form feeds each input and its residual against the same weight), as the
+ * tensor-core inference computes; the backward pass treats the rounding as
+ * identity.
  * quant == 1: GELU exact, then rounded to bfloat16 (the GPU's FP32 GELU);
  * quant == 2: the activation as the GPU's training forward pass and its
  * tcgen05 inference compute it: for units j with j % 8 < 6 the GELU in packed
@@ -107,7 +110,11 @@ double or_mlp_loss_grad(const double* P, const double* X, const double* T, int B
     double loss = 0.0;
     for (int s = 0; s < B; ++s) {
         double h0[MLP_IN], z1[MLP_H], h1[MLP_H], z2[MLP_H], h2[MLP_H], z3[MLP_H], h3[MLP_H];
-        for (int k = 0; k < MLP_IN; ++k) h0[k] = quant ? bf16r(X[s * MLP_IN + k]) : X[s * MLP_IN + k];
+        /* quantised: each input as bf16(x) + bf16(x - bf16(x)), the network's first layer taking both */
+        for (int k = 0; k < MLP_IN; ++k) {
+            const double x = X[s * MLP_IN + k];
+            h0[k] = quant ? bf16r(x) + bf16r(x - bf16r(x)) : x;
+        }
         for (int j = 0; j < MLP_H; ++j) {
             double a = b1[j];
             for (int k = 0; k < MLP_IN; ++k) a += W1q[j * MLP_IN + k] * h0[k];

@@ -14,7 +14,8 @@
 //              carries each bias as bf16(b) and bf16(b - bf16(b)) in the two
 //              K columns that meet it, so the MMA adds the bias in FP32 to
 //              ~2^-16 relative and no epilogue instruction is spent on it.
-// Layer 1 reads its 7 inputs, a 1 and a 1 (the bias pair) from [64, 72).
+// Layer 1 reads its 7 inputs, a 1 and a 1 (the bias pair), then the BF16
+// residuals of inputs 0..5 (meeting the same weights) from [64, 72).
 //
 // Weight image (shared memory, bytes), each matrix N x K, K-major, in 8 x 8
 // core matrices without swizzle (LBO = 128 B along K, SBO = (K / 8) * 128 B
@@ -186,7 +187,8 @@ __device__ __forceinline__ void sur_tc_hidden(const SurTc& s) {
 }
 
 // Layers 1..4 after the caller stored this thread's layer-1 input row into
-// TMEM (8 BF16 pairs at TC_A: x0..x6, then 1, 1 for the bias, then zeros);
+// TMEM (8 BF16 pairs at TC_A: x0..x6, then 1, 1 for the bias, then the
+// residuals x_k - bf16(x_k) of x0..x5, then a zero);
 // leaves the 16 output columns in D.  Returns false if a wait gave up.
 template <int GM>
 __device__ __forceinline__ bool sur_tc_layers(SurTc& s) {

@@ -37,7 +37,11 @@ void sur_make_fragments(const float* P, uint2* frag, float* bias) {
     const L layers[4] = {{SUR_W1, SUR_IN, SUR_H, 1, 8, SUR_F1}, {SUR_W2, SUR_H, SUR_H, 4, 8, SUR_F2},
                          {SUR_W3, SUR_H, SUR_H, 4, 8, SUR_F3}, {SUR_W4, SUR_H, SUR_OUT, 4, 1, SUR_F4}};
     for (const L& l : layers) {
-        auto w = [&](int j, int k) { return k < l.kin ? P[l.w + j * l.kin + k] : 0.0f; };
+        // layer 1: K columns 8..15 carry the inputs' BF16 residuals, with the same weights
+        auto w = [&](int j, int k) {
+            if (l.fbase == SUR_F1 && k >= 8 && k < 8 + l.kin) k -= 8;
+            return k < l.kin ? P[l.w + j * l.kin + k] : 0.0f;
+        };
         for (int kt = 0; kt < l.kt; ++kt)
             for (int nt = 0; nt < l.nt; ++nt)
                 for (int lane = 0; lane < 32; ++lane) {
@@ -74,6 +78,8 @@ void sur_make_tc_image(const float* P, uint16_t* img) {
     for (int n = 0; n < SUR_H; ++n) {
         for (int k = 0; k < 7; ++k) put(TC_B1, TC_K1, n, k, P[SUR_W1 + n * SUR_IN + k]);
         put_bias(TC_B1, TC_K1, n, 7, P[SUR_B1 + n]);
+        // K columns 9..14: the BF16 residuals of inputs 0..5 (direction and normal), same weights
+        for (int k = 0; k < 6; ++k) put(TC_B1, TC_K1, n, 9 + k, P[SUR_W1 + n * SUR_IN + k]);
         for (int k = 0; k < SUR_H; ++k) {
             put(TC_B2, TC_KH, n, k, P[SUR_W2 + n * SUR_H + k]);
             put(TC_B3, TC_KH, n, k, P[SUR_W3 + n * SUR_H + k]);
@@ -216,7 +222,11 @@ __global__ void __launch_bounds__(256) k_sur_fwd_bwd(const float* __restrict__ P
     for (int e = tid; e < SUR_H; e += 256) { S.b[e] = P[SUR_B1 + e]; S.b[SUR_H + e] = P[SUR_B2 + e]; S.b[2 * SUR_H + e] = P[SUR_B3 + e]; }
     if (tid < SUR_OUT) S.b[3 * SUR_H + tid] = P[SUR_B4 + tid];
     const size_t base = first + size_t(blockIdx.x) * TRB;
-    for (int e = tid; e < TRB * SUR_IN; e += 256) S.h0[e] = bq(X[((base + e / SUR_IN) % n) * 8 + e % SUR_IN]);
+    // each input as the first layer sees it: bf16(x) + bf16 of its residual
+    for (int e = tid; e < TRB * SUR_IN; e += 256) {
+        const float x = X[((base + e / SUR_IN) % n) * 8 + e % SUR_IN];
+        S.h0[e] = bq(x) + bq(bf16_residual(x));
+    }
     __syncthreads();
 
     // hidden layers: thread (warp, lane) -> outputs j = lane, lane + 32 of samples warp + 8 i
@@ -365,7 +375,9 @@ __global__ void __launch_bounds__(128) k_sur_eval(const uint2* __restrict__ frag
         float x0[2] = {0, 0}, x1[2] = {0, 0};
         if (r0 < n) { x0[0] = X[r0 * 8 + 2 * t]; x0[1] = X[r0 * 8 + 2 * t + 1]; }
         if (r1 < n) { x1[0] = X[r1 * 8 + 2 * t]; x1[1] = X[r1 * 8 + 2 * t + 1]; }
-        const uint32_t a[4] = {pack_bf16x2(x0[0], x0[1]), pack_bf16x2(x1[0], x1[1]), 0u, 0u};
+        const uint32_t a[4] = {pack_bf16x2(x0[0], x0[1]), pack_bf16x2(x1[0], x1[1]),
+                               pack_bf16x2(bf16_residual(x0[0]), bf16_residual(x0[1])),
+                               pack_bf16x2(bf16_residual(x1[0]), bf16_residual(x1[1]))};
         float out[4];
         sur_mlp16(frag, bias, a, out);
         if (r0 < n) { Y[r0 * 8 + 2 * t] = out[0]; Y[r0 * 8 + 2 * t + 1] = out[1]; }
@@ -391,8 +403,12 @@ __global__ void __launch_bounds__(128) k_sur_eval_tc(const uint4* __restrict__ i
             x0 = reinterpret_cast<const float4*>(X)[row * 2];
             x1 = reinterpret_cast<const float4*>(X)[row * 2 + 1];
         }
+        // inputs 0..6, the bias pair (1, 1), the residuals of inputs 0..5
         const uint32_t in[8] = {pack_bf16x2(x0.x, x0.y), pack_bf16x2(x0.z, x0.w), pack_bf16x2(x1.x, x1.y),
-                                pack_bf16x2(x1.z, 1.0f), pack_bf16x2(1.0f, 0.0f), 0u, 0u, 0u};
+                                pack_bf16x2(x1.z, 1.0f), pack_bf16x2(1.0f, bf16_residual(x0.x)),
+                                pack_bf16x2(bf16_residual(x0.y), bf16_residual(x0.z)),
+                                pack_bf16x2(bf16_residual(x0.w), bf16_residual(x1.x)),
+                                pack_bf16x2(bf16_residual(x1.y), 0.0f)};
         float out[8];
         if (!sur_tc_forward<GM>(s, in, out)) break;
         if (row < n) {

@@ -12,6 +12,9 @@
 // pre-arranged per (layer, k-tile, n-tile, lane) as the B fragment each lane
 // holds (two 32-bit registers), so each MMA needs one 64-bit shared load.
 //
+// Layer 1 sees each input x as bf16(x) plus bf16(bf16_residual(x)), both
+// against the same weight (K columns 0..7 and 8..15).
+//
 // Parameter layout (FP32 master copy):
 //   W1[64][8] b1[64] W2[64][64] b2[64] W3[64][64] b3[64] W4[8][64] b4[8]
 // with W[out][in]; W1[.][7], W4[6..7][.] and b4[6..7] stay zero.
@@ -60,6 +63,14 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
     return *reinterpret_cast<const uint32_t*>(&v);
 }
 
+// x - bf16(x): the part of an input that its BF16 rounding drops (exact in
+// FP32).  The network's first layer takes each input twice, as bf16(x) and as
+// bf16 of this residual, against the same weight, so the inputs reach the
+// tensor cores with ~16 significant bits instead of 8.
+__host__ __device__ __forceinline__ float bf16_residual(float x) {
+    return x - __bfloat162float(__float2bfloat16_rn(x));
+}
+
 __device__ __forceinline__ float tanh_fast(float x) {
     float y;
     asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
@@ -82,8 +93,9 @@ __device__ __forceinline__ void mma_bf16_16816(float (&c)[4], const uint32_t (&a
 }
 
 // One 16-sample tile through the network.  a_in: this lane's A fragment of
-// the 16 x 16 input (rows g, g+8; columns 2 t, 2 t + 1 in registers 0 / 1,
-// columns 8 + 2 t, ... in registers 2 / 3, which are zero: 8 inputs).
+// the 16 x 16 input (rows g, g+8; columns 2 t, 2 t + 1 in registers 0 / 1:
+// the 8 inputs; columns 8 + 2 t, ... in registers 2 / 3: their BF16
+// residuals, which meet the same weights).
 // frag: the 76 x 32 B fragments (shared memory), bias: b1 b2 b3 b4.
 // Returns the lane's output accumulator: rows g (out[0..1]) and g + 8
 // (out[2..3]), output columns 2 t, 2 t + 1, with g = lane / 4, t = lane % 4.
