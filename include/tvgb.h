@@ -198,6 +198,9 @@ int tvgb_vote3(const float* in, int in_layout, unsigned s0, unsigned s1, unsigne
  *     TVGB_ERR_ARG;
  *   - the first call on a device looks up the array's device address
  *     (cudaGetSymbolAddress) and should come before any stream capture;
+ *     the lookup is repeated after the device's context changes (a
+ *     cudaDeviceReset, or another library resetting the primary context),
+ *     so that first call after a reset should also precede any capture;
  *   - every call shares the one array: calls whose work overlaps on the GPU
  *     (different streams, or host threads without ordering) race and must be
  *     serialised by the caller.  Nothing in the array needs zeroing: each

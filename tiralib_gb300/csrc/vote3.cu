@@ -1437,9 +1437,33 @@ constexpr int NOALLOC_MAX_DEVICES = 64;
 static std::mutex g_noalloc_mu;
 static bool g_noalloc_ready[NOALLOC_MAX_DEVICES];
 static NoallocScratch g_noalloc_addr[NOALLOC_MAX_DEVICES];
+static void* g_noalloc_ctx[NOALLOC_MAX_DEVICES];
 
-// Device addresses of the arrays on the current device, looked up once per
-// device (the array names are host-side stand-ins in host code).
+// The current CUDA context (driver API, looked up through the runtime since
+// the library links only the runtime); null if unavailable.
+static void* current_context() {
+    using GetCtx = int (*)(void**);
+    static std::once_flag once;
+    static GetCtx fn = nullptr;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<GetCtx>(p);
+        else
+            cudaGetLastError();
+    });
+    void* ctx = nullptr;
+    if (fn && fn(&ctx) != 0) ctx = nullptr;
+    return ctx;
+}
+
+// Device addresses of the arrays on the current device (the array names are
+// host-side stand-ins in host code), looked up on the first call in each
+// context of a device: a device reset (cudaDeviceReset, or another library
+// resetting the primary context) makes a new context, whose module copy of
+// the arrays may sit elsewhere, so the cached addresses follow the context.
 static int noalloc_scratch(NoallocScratch& s) {
     int dev = 0;
     TVGB_CUDA(cudaGetDevice(&dev));
@@ -1447,14 +1471,18 @@ static int noalloc_scratch(NoallocScratch& s) {
         set_error("tvgb_vote3_noalloc: device %d beyond the supported %d", dev, NOALLOC_MAX_DEVICES);
         return TVGB_ERR_UNSUPPORTED;
     }
+    // the caller's arrays were classified (cudaPointerGetAttributes) before this, so the device's context
+    // is current; without one the addresses are looked up again on every call
+    void* ctx = current_context();
     std::lock_guard<std::mutex> g(g_noalloc_mu);
-    if (!g_noalloc_ready[dev]) {
+    if (!g_noalloc_ready[dev] || !ctx || ctx != g_noalloc_ctx[dev]) {
         NoallocScratch a{};
         TVGB_CUDA(cudaGetSymbolAddress(reinterpret_cast<void**>(&a.stick), g_noalloc_stick));
         TVGB_CUDA(cudaGetSymbolAddress(reinterpret_cast<void**>(&a.plate), g_noalloc_plate));
         TVGB_CUDA(cudaGetSymbolAddress(reinterpret_cast<void**>(&a.ball), g_noalloc_ball));
         g_noalloc_addr[dev] = a;
         g_noalloc_ready[dev] = true;
+        g_noalloc_ctx[dev] = ctx;
     }
     s = g_noalloc_addr[dev];
     return TVGB_OK;
