@@ -207,6 +207,30 @@ __global__ void __launch_bounds__(EIG_BLOCK, PRECISE ? TVGB_EIG_MINB : 1) k_eig3
 constexpr int EIGW_QCAP = 64;          // queue entries per warp (at most 31 + 32 between drains)
 constexpr int EIGW_QF = 11;            // floats per entry: 6 entries, w0..w2, tile, key
 
+// The FP64 phase of one queue entry and its results in global memory.  Not
+// inlined: its FP64 registers are spent inside the call, and the FP32 tile
+// loop around it keeps the kernel's register budget.
+template <int EVEC_FMT>
+__device__ __noinline__ void eigw_finish(const float* __restrict__ e, float* __restrict__ evals,
+                                         float* __restrict__ evecs) {
+    const unsigned key = __float_as_uint(e[10]);
+    const size_t i = size_t(__float_as_uint(e[9])) * 32 + (key & 31u);
+    const int code = int((key >> 5) & 3u);
+    const bool hi = (key >> 7) & 1u;
+    const float w[3] = {e[6], e[7], e[8]};
+    float ev[3], v[9];
+    eig3_precise_fp64(e[0], e[1], e[2], e[3], e[4], e[5], w, hi, code, ev, v, v + 3, v + 6);
+    if (evals) { evals[i * 3] = ev[0]; evals[i * 3 + 1] = ev[1]; evals[i * 3 + 2] = ev[2]; }
+    if (EVEC_FMT == 1 && evecs)
+        for (int k = 0; k < 9; ++k) evecs[i * 9 + k] = v[k];
+    if (EVEC_FMT == 2 && evecs) {
+        float th, ph;
+        to_spherical_d(v, th, ph); evecs[i * 6] = th; evecs[i * 6 + 1] = ph;
+        to_spherical_d(v + 3, th, ph); evecs[i * 6 + 2] = th; evecs[i * 6 + 3] = ph;
+        to_spherical_d(v + 6, th, ph); evecs[i * 6 + 4] = th; evecs[i * 6 + 5] = ph;
+    }
+}
+
 template <int IN_LAYOUT, int EVEC_FMT>
 __global__ void __launch_bounds__(EIG_BLOCK, TVGB_EIG_MINB) k_eig3w(const float* __restrict__ in, size_t n,
                                                                       float* __restrict__ evals,
@@ -246,25 +270,7 @@ __global__ void __launch_bounds__(EIG_BLOCK, TVGB_EIG_MINB) k_eig3w(const float*
     };
     // FP64 phase of queue entries [q0, q0 + cnt) (one per lane), results written to global memory
     auto drain = [&](int q0, int cnt) {
-        if (lane < cnt) {
-            const float* e = sq + (q0 + lane) * EIGW_QF;
-            const unsigned key = __float_as_uint(e[10]);
-            const size_t i = size_t(__float_as_uint(e[9])) * 32 + (key & 31u);
-            const int code = int((key >> 5) & 3u);
-            const bool hi = (key >> 7) & 1u;
-            const float w[3] = {e[6], e[7], e[8]};
-            float ev[3], v[9];
-            eig3_precise_fp64(e[0], e[1], e[2], e[3], e[4], e[5], w, hi, code, ev, v, v + 3, v + 6);
-            if (evals) { evals[i * 3] = ev[0]; evals[i * 3 + 1] = ev[1]; evals[i * 3 + 2] = ev[2]; }
-            if (EVEC_FMT == 1 && evecs)
-                for (int k = 0; k < 9; ++k) evecs[i * 9 + k] = v[k];
-            if (EVEC_FMT == 2 && evecs) {
-                float th, ph;
-                to_spherical_d(v, th, ph); evecs[i * 6] = th; evecs[i * 6 + 1] = ph;
-                to_spherical_d(v + 3, th, ph); evecs[i * 6 + 2] = th; evecs[i * 6 + 3] = ph;
-                to_spherical_d(v + 6, th, ph); evecs[i * 6 + 4] = th; evecs[i * 6 + 5] = ph;
-            }
-        }
+        if (lane < cnt) eigw_finish<EVEC_FMT>(sq + (q0 + lane) * EIGW_QF, evals, evecs);
         refined += unsigned(cnt);
     };
 
