@@ -397,7 +397,7 @@ __device__ __forceinline__ float narrow_trunc(double x) {
 // is completed in FP32.  41 FP64 arithmetic operations, and two conversions
 // (the pair's eigenvalues to FP32).
 // code 2: cyclic Jacobi on the whole matrix in FP64.
-__device__ __noinline__ void eig3_jacobi_fp64(float a, float b, float c, float d, float e, float f, float unsc,
+static __device__ __noinline__ void eig3_jacobi_fp64(float a, float b, float c, float d, float e, float f, float unsc,
                                               float* ev, float* v0, float* v1, float* v2);
 
 __device__ __forceinline__ void eig3_precise_fp64(float a, float b, float c, float d, float e, float f, const float* w,
@@ -490,7 +490,7 @@ __device__ __forceinline__ void eig3_precise_fp64(float a, float b, float c, flo
 // no eigenvalue is isolated (a near-triple cluster): cyclic Jacobi in FP64 on
 // the scaled matrix.  Rare; kept out of line so that its FP64 matrices do not
 // weigh on the register budget of its callers.
-__device__ __noinline__ void eig3_jacobi_fp64(float a, float b, float c, float d, float e, float f, float unsc,
+static __device__ __noinline__ void eig3_jacobi_fp64(float a, float b, float c, float d, float e, float f, float unsc,
                                               float* ev, float* v0, float* v1, float* v2) {
     const double A[6] = {double(a), double(b), double(d), double(c), double(e), double(f)};
     double M[3][3] = {{A[0], A[1], A[2]}, {A[1], A[3], A[4]}, {A[2], A[4], A[5]}};
