@@ -397,9 +397,6 @@ __device__ __forceinline__ float narrow_trunc(double x) {
 // is completed in FP32.  41 FP64 arithmetic operations, and two conversions
 // (the pair's eigenvalues to FP32).
 // code 2: cyclic Jacobi on the whole matrix in FP64.
-static __device__ __noinline__ void eig3_jacobi_fp64(float a, float b, float c, float d, float e, float f, float unsc,
-                                              float* ev, float* v0, float* v1, float* v2);
-
 __device__ __forceinline__ void eig3_precise_fp64(float a, float b, float c, float d, float e, float f, const float* w,
                                                   bool iso_high, int code, float* ev, float* v0, float* v1, float* v2) {
     const float amax = fmaxf(fmaxf(fmaxf(fabsf(a), fabsf(b)), fmaxf(fabsf(c), fabsf(d))), fmaxf(fabsf(e), fabsf(f)));
@@ -484,15 +481,8 @@ __device__ __forceinline__ void eig3_precise_fp64(float a, float b, float c, flo
         assemble<float>(iso_high, lw, w, lx, ly, x, y, ev, v0, v1, v2, unsc);
         return;
     }
-    eig3_jacobi_fp64(a * sc, b * sc, c * sc, d * sc, e * sc, f * sc, unsc, ev, v0, v1, v2);
-}
-
-// no eigenvalue is isolated (a near-triple cluster): cyclic Jacobi in FP64 on
-// the scaled matrix.  Rare; kept out of line so that its FP64 matrices do not
-// weigh on the register budget of its callers.
-static __device__ __noinline__ void eig3_jacobi_fp64(float a, float b, float c, float d, float e, float f, float unsc,
-                                              float* ev, float* v0, float* v1, float* v2) {
-    const double A[6] = {double(a), double(b), double(d), double(c), double(e), double(f)};
+    const double A[6] = {double(a * sc), double(b * sc), double(d * sc), double(c * sc), double(e * sc), double(f * sc)};
+    // no eigenvalue is isolated (a near-triple cluster): cyclic Jacobi in FP64
     double M[3][3] = {{A[0], A[1], A[2]}, {A[1], A[3], A[4]}, {A[2], A[4], A[5]}};
     double Q[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
     for (int sweep = 0; sweep < 8; ++sweep) {

@@ -12,16 +12,14 @@
 // two input tiles in shared memory: the next tile's copy (cp.async) runs
 // while the current one is solved.
 //
-// Precise mode: a scale-invariant FP32 solve for every tensor; tensors whose
-// remaining pair is closer than 1e-4 |lambda_max| are appended to a queue in
-// shared memory, and after a barrier the block's first threads finish the
-// queue in FP64, one flagged tensor per thread, reading the tensor from the
-// tile still in shared memory and writing their results into the tile's
-// output buffers before the coalesced store.  Each tensor is read from HBM
-// once and each result written once, and the FP64 pipe only sees flagged
-// tensors (27% of the C3 recipe's), packed into whole warps.  While a block
-// drains its queue with a few warps, the other resident blocks keep the SM
-// issuing FP32 work.
+// Precise mode (k_eig3w): a scale-invariant FP32 solve for every tensor;
+// tensors whose remaining pair is closer than 1e-4 |lambda_max| go to a
+// per-warp queue in shared memory, which the warp finishes in FP64, 32 at a
+// time, while the other warps go on with their FP32 work (no block-wide
+// barrier).  Each tensor is read from HBM once and each result written once
+// (the FP64 results overwrite their FP32 placeholders a few tiles later,
+// normally still in L2), and the FP64 pipe only sees flagged tensors (27% of
+// the C3 recipe's), packed into whole warps.
 #include "tvgb_common.cuh"
 #include "eig_device.cuh"
 #include <algorithm>
@@ -30,10 +28,11 @@
 namespace tvgb {
 
 constexpr int EIG_BLOCK = 256;
-// resident blocks per SM the precise kernel is compiled for: its FP64 phase
-// would otherwise take the register count past 64 per thread
+// resident blocks per SM the precise kernel is compiled for: 3 (80 registers,
+// almost no spills) measured faster than 4 or 5 (64 / 48 registers, with the
+// FP64 phase spilling): 4.24 ms against 4.67 / 4.81 ms for 2^27 tensors
 #ifndef TVGB_EIG_MINB
-#define TVGB_EIG_MINB 5
+#define TVGB_EIG_MINB 3
 #endif
 
 // in_layout: 9 (mat3 AoS), 6 (sym6 AoS), 60 (sym6 planes)
@@ -79,46 +78,39 @@ __device__ __forceinline__ void store_tile(float* __restrict__ dst, const float*
     }
 }
 
-// EVEC_FMT: 0 none, 1 cartesian (9), 2 spherical (6).  EVALS_IN: take the
-// eigenvalues from `evals_in` (the reference's evecs3spherical contract).
-// Shared-memory queue record of a tensor left to the FP64 phase: (slot in the
-// tile | code << 28 | isolated-high << 30, w0, w1, w2).
-template <int IN_LAYOUT, int EVEC_FMT, bool PRECISE, bool EVALS_IN>
-__global__ void __launch_bounds__(EIG_BLOCK, PRECISE ? TVGB_EIG_MINB : 1) k_eig3(const float* __restrict__ in, size_t n, size_t first, size_t last,
-                                                      const float* __restrict__ evals_in, float* __restrict__ evals,
-                                                      float* __restrict__ evecs,
-                                                      unsigned long long* __restrict__ n_refined, int aligned_in,
-                                                      int aligned_out) {
+// Parity mode (eigen.h's closed forms).  EVEC_FMT: 0 none, 1 cartesian (9),
+// 2 spherical (6).  EVALS_IN: take the eigenvalues from `evals_in` (the
+// reference's evecs3spherical contract).
+template <int IN_LAYOUT, int EVEC_FMT, bool EVALS_IN>
+__global__ void __launch_bounds__(EIG_BLOCK) k_eig3(const float* __restrict__ in, size_t n,
+                                                    const float* __restrict__ evals_in, float* __restrict__ evals,
+                                                    float* __restrict__ evecs, int aligned_in, int aligned_out) {
     constexpr int NF = IN_LAYOUT == 9 ? 9 : 6;
     constexpr int NV = EVEC_FMT == 1 ? 9 : (EVEC_FMT == 2 ? 6 : 0);
     __shared__ __align__(16) float s_in2[2][EIG_BLOCK * NF];   // the current tile and the next one
     __shared__ __align__(16) float s_ev[EIG_BLOCK * 3];
     __shared__ __align__(16) float s_vec[EIG_BLOCK * 9];
-    __shared__ uint4 s_q[PRECISE ? EIG_BLOCK : 1];
-    __shared__ unsigned s_qn;
-    unsigned refined = 0;   // thread 0: flagged tensors of this block
 
     const size_t stride = size_t(gridDim.x) * EIG_BLOCK;
     // tile at `base` into buffer `buf`: asynchronous when full, aligned and AoS
     auto fetch = [&](size_t base, int buf) {
-        const int cnt = int(min(size_t(EIG_BLOCK), last - base));
+        const int cnt = int(min(size_t(EIG_BLOCK), n - base));
         if (IN_LAYOUT != 60 && aligned_in && cnt == EIG_BLOCK)
             load_tile_async(in + base * NF, EIG_BLOCK * NF, s_in2[buf]);
         else
             load_tile<IN_LAYOUT>(in, n, base, cnt, s_in2[buf], aligned_in);
     };
     int it = 0;   // tiles done by this block: tile it sits in buffer it & 1
-    if (first + size_t(blockIdx.x) * EIG_BLOCK < last) fetch(first + size_t(blockIdx.x) * EIG_BLOCK, 0);
-    for (size_t base = first + size_t(blockIdx.x) * EIG_BLOCK; base < last; base += stride, ++it) {
-        const int cnt = int(min(size_t(EIG_BLOCK), last - base));
+    if (size_t(blockIdx.x) * EIG_BLOCK < n) fetch(size_t(blockIdx.x) * EIG_BLOCK, 0);
+    for (size_t base = size_t(blockIdx.x) * EIG_BLOCK; base < n; base += stride, ++it) {
+        const int cnt = int(min(size_t(EIG_BLOCK), n - base));
         const float* s_in = s_in2[it & 1];
-        if (PRECISE && threadIdx.x == 0) s_qn = 0;
         if (EVALS_IN)
             for (int i = threadIdx.x; i < cnt * 3; i += EIG_BLOCK) s_ev[i] = __ldg(evals_in + base * 3 + i);
         wait_tile_async();
         __syncthreads();
         // the other buffer was last read before the barrier that ended the previous tile
-        if (base + stride < last) fetch(base + stride, (it + 1) & 1);
+        if (base + stride < n) fetch(base + stride, (it + 1) & 1);
         const int t = threadIdx.x;
         if (t < cnt) {
             const float* m = s_in + t * NF;
@@ -126,45 +118,14 @@ __global__ void __launch_bounds__(EIG_BLOCK, PRECISE ? TVGB_EIG_MINB : 1) k_eig3
             if (NF == 9) { a = m[0]; b = m[1]; d = m[2]; c = m[4]; e = m[5]; f = m[8]; }
             else { a = m[0]; b = m[1]; d = m[2]; c = m[3]; e = m[4]; f = m[5]; }
             float ev[3], v[9];
-            if (PRECISE) {
-                float w[3];
-                bool hi;
-                const int code = eig3_precise_fp32(a, b, c, d, e, f, ev, v, v + 3, v + 6, w, hi);
-                if (code) {   // left to the FP64 phase below, which overwrites this slot's results
-                    const unsigned key = unsigned(t) | (unsigned(code) << 28) | ((hi ? 1u : 0u) << 30);
-                    s_q[atomicAdd(&s_qn, 1u)] = make_uint4(key, __float_as_uint(w[0]), __float_as_uint(w[1]),
-                                                           __float_as_uint(w[2]));
-                }
-            } else {
-                if (EVALS_IN) { ev[0] = s_ev[t * 3]; ev[1] = s_ev[t * 3 + 1]; ev[2] = s_ev[t * 3 + 2]; }
-                else eval3_d(a, b, c, d, e, f, ev[0], ev[1], ev[2]);
-                if (EVEC_FMT != 0) evec3_d(a, b, c, d, e, f, ev, v, v + 3, v + 6);
-            }
+            if (EVALS_IN) { ev[0] = s_ev[t * 3]; ev[1] = s_ev[t * 3 + 1]; ev[2] = s_ev[t * 3 + 2]; }
+            else eval3_d(a, b, c, d, e, f, ev[0], ev[1], ev[2]);
+            if (EVEC_FMT != 0) evec3_d(a, b, c, d, e, f, ev, v, v + 3, v + 6);
             if (!EVALS_IN) { s_ev[t * 3] = ev[0]; s_ev[t * 3 + 1] = ev[1]; s_ev[t * 3 + 2] = ev[2]; }
-            if (EVEC_FMT != 0 || PRECISE)
+            if (EVEC_FMT != 0)
                 for (int k = 0; k < 9; ++k) s_vec[t * 9 + k] = v[k];
         }
         __syncthreads();
-        if (PRECISE) {   // the tile's flagged tensors in FP64, packed into the first warps
-            const unsigned qn = s_qn;
-            if (threadIdx.x == 0) refined += qn;
-            if (threadIdx.x < qn) {
-                const uint4 r = s_q[threadIdx.x];
-                const int slot = int(r.x & 0x0FFFFFFFu);
-                const int code = int((r.x >> 28) & 3u);
-                const bool hi = (r.x >> 30) & 1u;
-                const float w[3] = {__uint_as_float(r.y), __uint_as_float(r.z), __uint_as_float(r.w)};
-                const float* m = s_in + slot * NF;
-                float a, b, c, d, e, f;
-                if (NF == 9) { a = m[0]; b = m[1]; d = m[2]; c = m[4]; e = m[5]; f = m[8]; }
-                else { a = m[0]; b = m[1]; d = m[2]; c = m[3]; e = m[4]; f = m[5]; }
-                float ev[3], v[9];
-                eig3_precise_fp64(a, b, c, d, e, f, w, hi, code, ev, v, v + 3, v + 6);
-                s_ev[slot * 3] = ev[0]; s_ev[slot * 3 + 1] = ev[1]; s_ev[slot * 3 + 2] = ev[2];
-                for (int k = 0; k < 9; ++k) s_vec[slot * 9 + k] = v[k];
-            }
-            __syncthreads();
-        }
         if (EVEC_FMT == 2) {
             // spherical output, packed 6 per tensor into the front of s_vec
             float sph[6];
@@ -185,7 +146,6 @@ __global__ void __launch_bounds__(EIG_BLOCK, PRECISE ? TVGB_EIG_MINB : 1) k_eig3
         if (NV && evecs) store_tile(evecs + base * NV, s_vec, cnt * NV, aligned_out, full);
         __syncthreads();
     }
-    if (PRECISE && n_refined && threadIdx.x == 0 && refined) atomicAdd(n_refined, (unsigned long long)refined);
 }
 
 // Precise mode, warp-tiled.  Each warp owns tiles of 32 consecutive tensors
@@ -206,30 +166,6 @@ __global__ void __launch_bounds__(EIG_BLOCK, PRECISE ? TVGB_EIG_MINB : 1) k_eig3
 // the other warps issue the FP32 phase.
 constexpr int EIGW_QCAP = 64;          // queue entries per warp (at most 31 + 32 between drains)
 constexpr int EIGW_QF = 11;            // floats per entry: 6 entries, w0..w2, tile, key
-
-// The FP64 phase of one queue entry and its results in global memory.  Not
-// inlined: its FP64 registers are spent inside the call, and the FP32 tile
-// loop around it keeps the kernel's register budget.
-template <int EVEC_FMT>
-__device__ __noinline__ void eigw_finish(const float* __restrict__ e, float* __restrict__ evals,
-                                         float* __restrict__ evecs) {
-    const unsigned key = __float_as_uint(e[10]);
-    const size_t i = size_t(__float_as_uint(e[9])) * 32 + (key & 31u);
-    const int code = int((key >> 5) & 3u);
-    const bool hi = (key >> 7) & 1u;
-    const float w[3] = {e[6], e[7], e[8]};
-    float ev[3], v[9];
-    eig3_precise_fp64(e[0], e[1], e[2], e[3], e[4], e[5], w, hi, code, ev, v, v + 3, v + 6);
-    if (evals) { evals[i * 3] = ev[0]; evals[i * 3 + 1] = ev[1]; evals[i * 3 + 2] = ev[2]; }
-    if (EVEC_FMT == 1 && evecs)
-        for (int k = 0; k < 9; ++k) evecs[i * 9 + k] = v[k];
-    if (EVEC_FMT == 2 && evecs) {
-        float th, ph;
-        to_spherical_d(v, th, ph); evecs[i * 6] = th; evecs[i * 6 + 1] = ph;
-        to_spherical_d(v + 3, th, ph); evecs[i * 6 + 2] = th; evecs[i * 6 + 3] = ph;
-        to_spherical_d(v + 6, th, ph); evecs[i * 6 + 4] = th; evecs[i * 6 + 5] = ph;
-    }
-}
 
 template <int IN_LAYOUT, int EVEC_FMT>
 __global__ void __launch_bounds__(EIG_BLOCK, TVGB_EIG_MINB) k_eig3w(const float* __restrict__ in, size_t n,
@@ -270,7 +206,25 @@ __global__ void __launch_bounds__(EIG_BLOCK, TVGB_EIG_MINB) k_eig3w(const float*
     };
     // FP64 phase of queue entries [q0, q0 + cnt) (one per lane), results written to global memory
     auto drain = [&](int q0, int cnt) {
-        if (lane < cnt) eigw_finish<EVEC_FMT>(sq + (q0 + lane) * EIGW_QF, evals, evecs);
+        if (lane < cnt) {
+            const float* e = sq + (q0 + lane) * EIGW_QF;
+            const unsigned key = __float_as_uint(e[10]);
+            const size_t i = size_t(__float_as_uint(e[9])) * 32 + (key & 31u);
+            const int code = int((key >> 5) & 3u);
+            const bool hi = (key >> 7) & 1u;
+            const float w[3] = {e[6], e[7], e[8]};
+            float ev[3], v[9];
+            eig3_precise_fp64(e[0], e[1], e[2], e[3], e[4], e[5], w, hi, code, ev, v, v + 3, v + 6);
+            if (evals) { evals[i * 3] = ev[0]; evals[i * 3 + 1] = ev[1]; evals[i * 3 + 2] = ev[2]; }
+            if (EVEC_FMT == 1 && evecs)
+                for (int k = 0; k < 9; ++k) evecs[i * 9 + k] = v[k];
+            if (EVEC_FMT == 2 && evecs) {
+                float th, ph;
+                to_spherical_d(v, th, ph); evecs[i * 6] = th; evecs[i * 6 + 1] = ph;
+                to_spherical_d(v + 3, th, ph); evecs[i * 6 + 2] = th; evecs[i * 6 + 3] = ph;
+                to_spherical_d(v + 6, th, ph); evecs[i * 6 + 4] = th; evecs[i * 6 + 5] = ph;
+            }
+        }
         refined += unsigned(cnt);
     };
 
@@ -426,20 +380,15 @@ static int launch_eig3_t(const float* in, size_t n, const float* ev_in, float* e
                          cudaStream_t s) {
     const int ai = (reinterpret_cast<uintptr_t>(in) % 16) == 0;
     const int ao = (!ev || reinterpret_cast<uintptr_t>(ev) % 16 == 0) && (!vec || reinterpret_cast<uintptr_t>(vec) % 16 == 0);
-    if (PR && !EI) {   // precise: the warp-tiled kernel
-        KernelTimer kt_("k_eig3", s);
+    KernelTimer kt_("k_eig3", s);
+    if constexpr (PR) {   // precise: the warp-tiled kernel
         k_eig3w<IL, EF><<<resident_grid(k_eig3w<IL, EF>, EIG_BLOCK, n), EIG_BLOCK, 0, s>>>(in, n, ev, vec, nref, ai,
                                                                                             ao);
-        kt_.stop();
-        TVGB_LAUNCHED();
-        return TVGB_OK;
+    } else {
+        k_eig3<IL, EF, EI><<<resident_grid(k_eig3<IL, EF, EI>, EIG_BLOCK, n), EIG_BLOCK, 0, s>>>(in, n, ev_in, ev, vec,
+                                                                                                ai, ao);
     }
-    {
-        KernelTimer kt_("k_eig3", s);
-        k_eig3<IL, EF, PR, EI><<<resident_grid(k_eig3<IL, EF, PR, EI>, EIG_BLOCK, n), EIG_BLOCK, 0, s>>>(
-            in, n, 0, n, ev_in, ev, vec, PR ? nref : nullptr, ai, ao);
-        kt_.stop();
-    }
+    kt_.stop();
     TVGB_LAUNCHED();
     return TVGB_OK;
 }

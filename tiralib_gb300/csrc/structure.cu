@@ -66,6 +66,8 @@ struct StArgs {
     float g[MAXK];
     float* out;
     int layout;
+    float2 g2[13];        // (g, g) pairs and (g / 4, g / 4) pairs, for the packed blurs of the TMA kernel
+    float2 gz2[13];
 };
 
 // d/d(axis) at an in-volume voxel: volume<T>::gradient's rule
@@ -236,13 +238,13 @@ __device__ __forceinline__ void st_zdispatch(int j, float (&acc)[6][K], const fl
 
 // the z window of k_st3t: 3 channels of two x outputs as packed partial sums
 template <int K, int J>
-__device__ __forceinline__ void st_zstep2(float2 (&acc)[3][K], const float2 (&v)[3], const float (&gw)[K],
+__device__ __forceinline__ void st_zstep2(float2 (&acc)[3][K], const float2 (&v)[3], const float2* gw2,
                                           float2 (&done)[3]) {
 #pragma unroll
     for (int m = 0; m < K; ++m) {
         const int sl = (J - m + K) % K;
 #pragma unroll
-        for (int o = 0; o < 3; ++o) acc[o][sl] = __ffma2_rn(make_float2(gw[m], gw[m]), v[o], acc[o][sl]);
+        for (int o = 0; o < 3; ++o) acc[o][sl] = __ffma2_rn(gw2[m], v[o], acc[o][sl]);
     }
     constexpr int sd = (J + 1) % K;
 #pragma unroll
@@ -250,7 +252,7 @@ __device__ __forceinline__ void st_zstep2(float2 (&acc)[3][K], const float2 (&v)
 }
 
 template <int K>
-__device__ __forceinline__ void st_zdispatch2(int j, float2 (&acc)[3][K], const float2 (&v)[3], const float (&gw)[K],
+__device__ __forceinline__ void st_zdispatch2(int j, float2 (&acc)[3][K], const float2 (&v)[3], const float2* gw,
                                               float2 (&done)[3]) {
 #define TVGB_ZCASE2(J) \
     case J:            \
@@ -467,6 +469,9 @@ __global__ void __launch_bounds__(STX * STY, 2) k_st3(StArgs a) {
 // rows sY[6][8][SP].  Product column px (0 .. EX - 1, global x = ox0 - off +
 // px) is stored at index px + p0 of its row, where p0 (0 or 1) makes the
 // pairs that start at an even index line up with 8-byte aligned raw pairs.
+#ifndef TVGB_ST3T_MINB
+#define TVGB_ST3T_MINB 2       // resident CTAs per SM the TMA kernel's registers are sized for
+#endif
 constexpr int ST_TMA_SLOTS = 8, ST_TMA_AHEAD = 6;   // slots >= ahead + 2: a slot is reused two planes after its last read
 constexpr uint32_t ST_TMA_WAIT_LIMIT = 1u << 24;    // mbarrier polls before a CTA gives up
 
@@ -498,7 +503,7 @@ static __device__ unsigned g_st3_faults;             // CTAs whose plane wait ti
 __device__ __forceinline__ float2 f2(float x) { return make_float2(x, x); }
 
 template <int K>
-__global__ void __launch_bounds__(STX * STY, 2) k_st3t(const __grid_constant__ CUtensorMap vmap, StArgs a) {
+__global__ void __launch_bounds__(STX * STY, TVGB_ST3T_MINB) k_st3t(const __grid_constant__ CUtensorMap vmap, StArgs a) {
     using G = St3Geom<K>;
     extern __shared__ __align__(128) float smem[];
     float* raw = smem;
@@ -544,10 +549,7 @@ __global__ void __launch_bounds__(STX * STY, 2) k_st3t(const __grid_constant__ C
     // face rules: per task column / row weights (hi, centre, lo); inner CTAs need none
     const bool inner = ox0 - a.off - 1 >= 0 && ox0 - a.off + G::EX < a.s2 && oy0 - a.off - 1 >= 0 &&
                        oy0 - a.off + G::EY < a.s1;
-    // blur weights; z weights carry the 1/4 of the doubled gradients
-    float gw[K], gz[K];
-#pragma unroll
-    for (int k = 0; k < K; ++k) { gw[k] = a.g[k]; gz[k] = 0.25f * a.g[k]; }
+    // blur weights (kernel parameters, read where used); the z weights carry the 1/4 of the doubled gradients
     // x blur / z window / output: channels 3 h .. 3 h + 2 at (x0, x0 + 1) of row ty
     const int h = tid >> 7, ty = (tid >> 4) & 7, px = (tid & 15) * 2;
     const int y = oy0 + ty, x0 = ox0 + px;
@@ -631,7 +633,7 @@ __global__ void __launch_bounds__(STX * STY, 2) k_st3t(const __grid_constant__ C
             for (int o = 0; o < 4; ++o) {
                 float2 s2 = make_float2(0.0f, 0.0f);
 #pragma unroll
-                for (int k = 0; k < K; ++k) s2 = __ffma2_rn(f2(gw[k]), v[o + k], s2);
+                for (int k = 0; k < K; ++k) s2 = __ffma2_rn(a.g2[k], v[o + k], s2);
                 dst[o * (G::SP / 2)] = s2;
             }
         }
@@ -650,14 +652,14 @@ __global__ void __launch_bounds__(STX * STY, 2) k_st3t(const __grid_constant__ C
                 if (p0 == 0) {
 #pragma unroll
                     for (int k = 0; k < K; ++k) {
-                        if ((k & 1) == 0) s2 = __ffma2_rn(f2(gw[k]), w[k / 2], s2);
-                        else { s2.x = fmaf(gw[k], w[k / 2].y, s2.x); s2.y = fmaf(gw[k], w[k / 2 + 1].x, s2.y); }
+                        if ((k & 1) == 0) s2 = __ffma2_rn(a.g2[k], w[k / 2], s2);
+                        else { s2.x = fmaf(a.g[k], w[k / 2].y, s2.x); s2.y = fmaf(a.g[k], w[k / 2 + 1].x, s2.y); }
                     }
                 } else {
 #pragma unroll
                     for (int k = 0; k < K; ++k) {
-                        if ((k & 1) == 1) s2 = __ffma2_rn(f2(gw[k]), w[(k + 1) / 2], s2);
-                        else { s2.x = fmaf(gw[k], w[k / 2].y, s2.x); s2.y = fmaf(gw[k], w[k / 2 + 1].x, s2.y); }
+                        if ((k & 1) == 1) s2 = __ffma2_rn(a.g2[k], w[(k + 1) / 2], s2);
+                        else { s2.x = fmaf(a.g[k], w[k / 2].y, s2.x); s2.y = fmaf(a.g[k], w[k / 2 + 1].x, s2.y); }
                     }
                 }
                 v[cc] = s2;
@@ -668,7 +670,7 @@ __global__ void __launch_bounds__(STX * STY, 2) k_st3t(const __grid_constant__ C
         }
         // z window: plane iz feeds the K outputs oz = iz + off - m, m = 0 .. K - 1; slot (iz - iz_lo) % K
         float2 done[3];
-        st_zdispatch2<K>((iz - iz_lo) % K, acc, v, gz, done);
+        st_zdispatch2<K>((iz - iz_lo) % K, acc, v, a.gz2, done);
         const int oz = iz - (K - 1) + a.off;
         if (oz >= oz_lo && y < a.o1 && x0 < a.o2) {
             const size_t idx = (size_t(oz) * a.o1 + y) * a.o2 + x0;
@@ -725,6 +727,10 @@ int structure_tensor3_device(const float* vol, unsigned s0, unsigned s1, unsigne
     a.o0 = int(d[0]); a.o1 = int(d[1]); a.o2 = int(d[2]);
     a.K = int(K); a.off = mode == 0 ? 0 : int(K / 2);
     gaussian1d(K, sigma, a.g);
+    for (unsigned k = 0; k < K && k < 13; ++k) {
+        a.g2[k] = make_float2(a.g[k], a.g[k]);
+        a.gz2[k] = make_float2(0.25f * a.g[k], 0.25f * a.g[k]);
+    }
     a.out = out; a.layout = out_layout;
     const unsigned gx = ceil_div(d[2], STX), gy = ceil_div(d[1], STY);
     const bool fixed = K <= unsigned(ST_MAXT);
