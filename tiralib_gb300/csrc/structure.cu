@@ -7,14 +7,18 @@
 // passes, cuda_convolve3z/3y/3x :275,259,243) with the kernel in global
 // memory, intermediates in HBM and a device synchronise after each pass.
 //
-// Here one kernel does it all: a CTA owns a 32 x 8 output column and marches
-// through the input z-planes, keeping the last three raw planes (with a
-// one-voxel halo) in shared memory so each input value is read from HBM about
-// once; per plane it forms the gradient (central inside, one-sided at the
-// faces), the six products on the haloed xy region, blurs them along y then x
-// in shared memory, and keeps the last K blurred planes in a shared-memory
-// ring from which each finished output plane is blurred along z and written
-// once.  HBM traffic ~ one read of the volume plus one write of the six
+// Here one kernel does it all (k_st3<K> for K = 3..13 taps, k_st3_any
+// above): a CTA owns a 32 x 8 output column and marches through the input
+// z-planes.  Per plane it forms the gradients (central inside, one-sided at
+// the faces) and their six products on the haloed xy tile from the last three
+// raw planes in shared memory, blurs them along y (one thread per channel and
+// column, the column held in registers) and along x (64-bit row loads), and
+// feeds each thread's two x outputs of three channels into a register window
+// of K partial sums per output, which completes the z blur: each finished
+// output plane is written once.  The raw planes are staged either by each
+// thread's own loads one plane ahead (k_st3) or, for volumes whose rows meet
+// the TMA rules, by cp.async.bulk.tensor boxes issued six planes ahead
+// (k_st3_tma).  HBM traffic ~ one read of the volume plus one write of the six
 // components (28 B per voxel).
 //
 // tvgb_gaussian_filter3d / tvgb_gaussian_convolve2 keep the reference's
@@ -66,8 +70,6 @@ struct StArgs {
     float g[MAXK];
     float* out;
     int layout;
-    float2 g2[13];        // (g, g) pairs and (g / 4, g / 4) pairs, for the packed blurs of the TMA kernel
-    float2 gz2[13];
 };
 
 // d/d(axis) at an in-volume voxel: volume<T>::gradient's rule
@@ -234,36 +236,6 @@ __device__ __forceinline__ void st_zdispatch(int j, float (&acc)[6][K], const fl
         default: break;
     }
 #undef TVGB_ZCASE
-}
-
-// the z window of k_st3t: 3 channels of two x outputs as packed partial sums
-template <int K, int J>
-__device__ __forceinline__ void st_zstep2(float2 (&acc)[3][K], const float2 (&v)[3], const float2* gw2,
-                                          float2 (&done)[3]) {
-#pragma unroll
-    for (int m = 0; m < K; ++m) {
-        const int sl = (J - m + K) % K;
-#pragma unroll
-        for (int o = 0; o < 3; ++o) acc[o][sl] = __ffma2_rn(gw2[m], v[o], acc[o][sl]);
-    }
-    constexpr int sd = (J + 1) % K;
-#pragma unroll
-    for (int o = 0; o < 3; ++o) { done[o] = acc[o][sd]; acc[o][sd] = make_float2(0.0f, 0.0f); }
-}
-
-template <int K>
-__device__ __forceinline__ void st_zdispatch2(int j, float2 (&acc)[3][K], const float2 (&v)[3], const float2* gw,
-                                              float2 (&done)[3]) {
-#define TVGB_ZCASE2(J) \
-    case J:            \
-        if constexpr (J < K) st_zstep2<K, J>(acc, v, gw, done); \
-        break;
-    switch (j) {
-        TVGB_ZCASE2(0) TVGB_ZCASE2(1) TVGB_ZCASE2(2) TVGB_ZCASE2(3) TVGB_ZCASE2(4) TVGB_ZCASE2(5) TVGB_ZCASE2(6)
-        TVGB_ZCASE2(7) TVGB_ZCASE2(8) TVGB_ZCASE2(9) TVGB_ZCASE2(10) TVGB_ZCASE2(11) TVGB_ZCASE2(12)
-        default: break;
-    }
-#undef TVGB_ZCASE2
 }
 
 // twice volume<T>::gradient's rule (central difference inside, one-sided at
@@ -447,90 +419,78 @@ __global__ void __launch_bounds__(STX * STY, 2) k_st3(StArgs a) {
     }
 }
 
-// ------------------------------------------------------------------ TMA-staged kernel
-// The same computation as k_st3 with fewer instructions per voxel, for
-// volumes whose rows are 16-byte multiples (s2 % 4 == 0) and 16-byte
-// aligned (the TMA rules):
-//   * each raw z-plane tile (with its halo) arrives in shared memory by one
-//     cp.async.bulk.tensor box, issued by one thread ST_TMA_AHEAD planes
-//     ahead into a ring of ST_TMA_SLOTS slots with one mbarrier each; no
-//     registers or load instructions of the other threads are spent on it,
-//     and voxels outside the volume read as zero;
-//   * gradients and products are formed for pairs of neighbouring x columns
-//     with packed FP32 instructions (FADD2 / FFMA2 / FMUL2) and 64-bit
-//     shared-memory accesses; the face rules of volume<T>::gradient enter as
-//     per-point weights (hi, centre, lo) of the three samples;
-//   * the y blur runs on column pairs (FFMA2), 4 output rows per thread;
-//   * the x blur pairs even taps (FFMA2 on an aligned pair) with odd taps
-//     (two FFMA);
-//   * the z blur keeps each thread's two x outputs of 3 channels as K
-//     packed partial sums (FFMA2).
-// Shared memory: the raw ring, the products sT[6][EY][SP] and the y-blurred
-// rows sY[6][8][SP].  Product column px (0 .. EX - 1, global x = ox0 - off +
-// px) is stored at index px + p0 of its row, where p0 (0 or 1) makes the
-// pairs that start at an even index line up with 8-byte aligned raw pairs.
-#ifndef TVGB_ST3T_MINB
-#define TVGB_ST3T_MINB 2       // resident CTAs per SM the TMA kernel's registers are sized for
-#endif
+// ------------------------------------------------------------------ TMA-staged raw planes
+// k_st3 with its raw z-planes staged by the Tensor Memory Accelerator, for
+// volumes whose rows meet the TMA rules (s2 % 4 == 0, 16-byte aligned): one
+// thread issues a cp.async.bulk.tensor box per plane (the tile with its halo,
+// zero outside the volume) ST_TMA_AHEAD planes ahead into a ring of
+// ST_TMA_SLOTS slots with one mbarrier each.  The other threads spend no
+// registers or load instructions on the staging and wait only on the
+// mbarrier; one block barrier per plane goes (two remain).  Every wait is
+// bounded: a wait that runs out ends the CTA's loop at its next barrier and
+// thread 0 waits, bounded, for the copies still in flight before the CTA
+// exits (g_st3_faults counts such CTAs).
 constexpr int ST_TMA_SLOTS = 8, ST_TMA_AHEAD = 6;   // slots >= ahead + 2: a slot is reused two planes after its last read
 constexpr uint32_t ST_TMA_WAIT_LIMIT = 1u << 24;    // mbarrier polls before a CTA gives up
 
 template <int K>
-struct St3Geom {
+struct St3TmaGeom {
     static constexpr int EX = STX + K - 1, EY = STY + K - 1;
-    // box width: the pairs reach raw column EX + 4 - p0 past the shift r <= 3
-    static constexpr int BX = (EX + 8 + 3) / 4 * 4;
+    static constexpr int BX = (EX + 2 + 3 + 3) / 4 * 4;  // box width: raw columns EX + 2 after a shift rs <= 3
     static constexpr int BY = EY + 2;
     static constexpr int SLOT = (BX * BY + 31) / 32 * 32;   // floats per ring slot (128-byte multiples)
-    static constexpr int SP = EX + 2;                   // sT / sY row pitch (even)
-    static constexpr int NPJ = EX / 2 + 1;              // column pairs of a product / blurred row
-    // raw ring, sT, sY, then the slots' mbarriers (the ring starts the 128-byte aligned dynamic region)
+    static constexpr uint32_t BOX_BYTES = uint32_t(BX) * BY * 4;
+    // raw ring, products sT[6][EY][EX], y-blurred rows sY[6][8][EX], then the slots' mbarriers
     static constexpr size_t SMEM =
-        sizeof(float) * (size_t(ST_TMA_SLOTS) * SLOT + 6 * EY * SP + 6 * STY * SP) + 8 * ST_TMA_SLOTS;
+        sizeof(float) * (size_t(ST_TMA_SLOTS) * SLOT + 6 * EY * EX + 6 * STY * EX) + 8 * ST_TMA_SLOTS;
 };
-
-// weights (hi, centre, lo) of volume<T>::gradient at position p of S samples,
-// doubled (the z weights carry 1 / 4); zero outside the volume
-__device__ __forceinline__ float3 grad_weights(int p, int S) {
-    if (p < 0 || p >= S || S < 2) return make_float3(0.0f, 0.0f, 0.0f);
-    if (p == 0) return make_float3(2.0f, -2.0f, 0.0f);
-    if (p == S - 1) return make_float3(0.0f, 2.0f, -2.0f);
-    return make_float3(1.0f, 0.0f, -1.0f);
-}
 
 static __device__ unsigned g_st3_faults;             // CTAs whose plane wait timed out
 
-__device__ __forceinline__ float2 f2(float x) { return make_float2(x, x); }
-
 template <int K>
-__global__ void __launch_bounds__(STX * STY, TVGB_ST3T_MINB) k_st3t(const __grid_constant__ CUtensorMap vmap, StArgs a) {
-    using G = St3Geom<K>;
+__global__ void __launch_bounds__(STX * STY, 2) k_st3_tma(const __grid_constant__ CUtensorMap vmap, StArgs a) {
+    static_assert(K <= ST_MAXT, "fixed-tap kernel");
+    constexpr int EX = STX + K - 1, EY = STY + K - 1;   // EX even: 64-bit row loads stay aligned
+    using G = St3TmaGeom<K>;
+    constexpr int RX = G::BX, RY = EY + 2;                // raw row pitch: the TMA box width
+    constexpr int NT = STX * STY;
+    constexpr int PS = EY * EX;                          // product points per plane
+    constexpr int NP = (PS + NT - 1) / NT;               // product points per thread
     extern __shared__ __align__(128) float smem[];
-    float* raw = smem;
+    float* raw = smem;                                   // ST_TMA_SLOTS slots of G::SLOT floats
     float* sT = raw + ST_TMA_SLOTS * G::SLOT;
-    float* sY = sT + 6 * G::EY * G::SP;
-    uint64_t* bars = reinterpret_cast<uint64_t*>(sY + 6 * STY * G::SP);   // 8-byte aligned: even float count
+    float* sY = sT + 6 * PS;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(sY + 6 * STY * EX);
     const int tid = threadIdx.x;
+    float gw[K], gz[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) { gw[k] = a.g[k]; gz[k] = 0.25f * a.g[k]; }
+
     const int ox0 = blockIdx.x * STX, oy0 = blockIdx.y * STY;
     const int oz_lo = blockIdx.z * a.zchunk, oz_hi = min(a.o0 - 1, oz_lo + a.zchunk - 1);
     const int iz_lo = oz_lo - a.off, iz_hi = oz_hi + K - 1 - a.off;
-    // raw tile: columns x = ox0 - off - 1 .. + EX + 1, rows y = oy0 - off - 1 .. + EY + 1; the box starts r
-    // columns further left so that its x coordinate is a multiple of 4
-    const int r = ((-a.off - 1) % 4 + 4) % 4;
-    const int p0 = (1 + r) & 1;
-    const int bx0 = ox0 - a.off - 1 - r, by0 = oy0 - a.off - 1;
-    const int P0 = iz_lo - 1, qmax = iz_hi + 1 - P0;     // raw planes P0 + q, q = 0 .. qmax
-    constexpr uint32_t BOX_BYTES = uint32_t(G::BX) * G::BY * 4;
+    const int ix0 = ox0 - a.off, iy0 = oy0 - a.off;
     const size_t on = size_t(a.o0) * a.o1 * a.o2;
+    const size_t plane = size_t(a.s1) * a.s2;
+    // every product point and its x/y neighbours inside the volume: no edge rules in x, y
+    const bool inner = ix0 >= 1 && ix0 + EX <= a.s2 - 1 && iy0 >= 1 && iy0 + EY <= a.s1 - 1;
 
-    if (tid == 0) {
+    // owned outputs: channels 3h..3h+2 at (x0 + {0,1}, y) of every plane
+    const int h = tid >> 7, ty = (tid >> 4) & 7, px = (tid & 15) * 2;
+    const int y = oy0 + ty, x0 = ox0 + px;
+
+    // raw tile: columns ix0 - 1 .. ix0 + EX, rows iy0 - 1 .. iy0 + EY; the box starts rs columns further left so
+    // that its x coordinate is a multiple of 4 (the TMA rule), and element (ry, rx) sits at ry * RX + rx + rs
+    const int rs = ((-a.off - 1) % 4 + 4) % 4;
+    const int bx0 = ix0 - 1 - rs, by0 = iy0 - 1;
+    const int P0 = iz_lo - 1, qmax = iz_hi + 1 - P0;     // raw planes P0 + q, q = 0 .. qmax
+    if (tid == 0)
         for (int i = 0; i < ST_TMA_SLOTS; ++i) tc::mbar_init(&bars[i], 1);
-    }
     __syncthreads();
     auto issue = [&](int q) {   // thread 0: raw plane P0 + q into slot q % SLOTS
         uint64_t* b = &bars[q % ST_TMA_SLOTS];
         tma::fence_proxy_async();
-        tma::arrive_expect_tx(b, BOX_BYTES);
+        tma::arrive_expect_tx(b, G::BOX_BYTES);
         tma::load_3d(raw + (q % ST_TMA_SLOTS) * G::SLOT, &vmap, bx0, by0, P0 + q, b);
     };
     if (tid == 0)
@@ -544,159 +504,126 @@ __global__ void __launch_bounds__(STX * STY, TVGB_ST3T_MINB) k_st3t(const __grid
     wait(0);
     wait(1);
 
-    // product tasks: (row py, column pair j) -> raw index of column px = 2 j - p0 (even), sT index 2 j
-    constexpr int TP = G::EY * G::NPJ;
-    // face rules: per task column / row weights (hi, centre, lo); inner CTAs need none
-    const bool inner = ox0 - a.off - 1 >= 0 && ox0 - a.off + G::EX < a.s2 && oy0 - a.off - 1 >= 0 &&
-                       oy0 - a.off + G::EY < a.s1;
-    // blur weights (kernel parameters, read where used); the z weights carry the 1/4 of the doubled gradients
-    // x blur / z window / output: channels 3 h .. 3 h + 2 at (x0, x0 + 1) of row ty
-    const int h = tid >> 7, ty = (tid >> 4) & 7, px = (tid & 15) * 2;
-    const int y = oy0 + ty, x0 = ox0 + px;
-    float2 acc[3][K];
+    float acc[6][K];
 #pragma unroll
-    for (int c = 0; c < 3; ++c)
+    for (int o = 0; o < 6; ++o)
 #pragma unroll
-        for (int k = 0; k < K; ++k) acc[c][k] = make_float2(0.0f, 0.0f);
+        for (int k = 0; k < K; ++k) acc[o][k] = 0.0f;
 
     int qfail = -1;
     for (int iz = iz_lo; iz <= iz_hi; ++iz) {
-        const int q = iz - P0;                           // this plane; its neighbours q - 1, q + 1
-        // the next plane ahead goes into the slot of plane q + AHEAD + 1 - SLOTS <= q - 2, last read before the
-        // barrier that followed the previous plane's products
+        const bool zin = iz >= 0 && iz < a.s0;
+        const int qz = iz - P0;                          // this plane's ring index; its neighbours qz - 1, qz + 1
+        // the plane ST_TMA_AHEAD ahead goes into the slot of plane qz + AHEAD - SLOTS <= qz - 2, last read by the
+        // products of the previous plane, before the barrier that followed them
         if (tid == 0 && issued < qmax) issue(++issued);
-        wait(q + 1);
-        const float* R0 = raw + ((q - 1) % ST_TMA_SLOTS) * G::SLOT;
-        const float* R1 = raw + (q % ST_TMA_SLOTS) * G::SLOT;
-        const float* R2 = raw + ((q + 1) % ST_TMA_SLOTS) * G::SLOT;
-        const float3 wz = grad_weights(iz, a.s0);
-        // ---- gradients and products of pairs (x, x + 1)
-        if (wz.x != 0.0f || wz.y != 0.0f || wz.z != 0.0f) {
+        wait(qz + 1);
+        if (zin) {
+            const float* R0 = raw + ((qz - 1) % ST_TMA_SLOTS) * G::SLOT + rs;
+            const float* R1 = raw + (qz % ST_TMA_SLOTS) * G::SLOT + rs;
+            const float* R2 = raw + ((qz + 1) % ST_TMA_SLOTS) * G::SLOT + rs;
+            if (inner && iz >= 1 && iz <= a.s0 - 2) {
 #pragma unroll
-            for (int i = 0; i < (TP + STX * STY - 1) / (STX * STY); ++i) {
-                const int t = tid + i * STX * STY;
-                if (t < TP) {
-                    const int py = t / G::NPJ, j = t - py * G::NPJ;
-                    const int pxc = 2 * j - p0;                          // product column
-                    const int c = (py + 1) * G::BX + pxc + 1 + r;       // even
-                    const float2 m = *reinterpret_cast<const float2*>(R1 + c);
-                    const float lo = R1[c - 1], hi = R1[c + 2];
-                    const float2 up = *reinterpret_cast<const float2*>(R1 + c + G::BX);
-                    const float2 dn = *reinterpret_cast<const float2*>(R1 + c - G::BX);
-                    const float2 zu = *reinterpret_cast<const float2*>(R2 + c);
-                    const float2 zd = *reinterpret_cast<const float2*>(R0 + c);
-                    float2 gx, gy;
-                    if (inner) {
-                        gx = make_float2(m.y - lo, hi - m.x);
-                        gy = __ffma2_rn(f2(-1.0f), dn, up);
-                    } else {
-                        const int gxp = ox0 - a.off + pxc, gyp = oy0 - a.off + py;
-                        const float3 wa = grad_weights(gxp, a.s2), wb = grad_weights(gxp + 1, a.s2);
-                        const float3 wy = grad_weights(gyp, a.s1);
-                        gx = make_float2(fmaf(wa.x, m.y, fmaf(wa.y, m.x, wa.z * lo)),
-                                         fmaf(wb.x, hi, fmaf(wb.y, m.y, wb.z * m.x)));
-                        gy = __ffma2_rn(f2(wy.x), up, __ffma2_rn(f2(wy.y), m, __fmul2_rn(f2(wy.z), dn)));
-                        const float zx = wy.x != 0.0f || wy.y != 0.0f || wy.z != 0.0f ? 1.0f : 0.0f;
-                        gx = __fmul2_rn(gx, f2(zx));   // rows outside the volume: no gradient at all
+                for (int q = 0; q < NP; ++q) {
+                    const int e = tid + q * NT;
+                    if (e < PS) {
+                        const int ry = e / EX, rx = e - ry * EX;
+                        const int c = (ry + 1) * RX + rx + 1;
+                        const float gx = R1[c + 1] - R1[c - 1];
+                        const float gy = R1[c + RX] - R1[c - RX];
+                        const float gzv = R2[c] - R0[c];
+                        sT[e] = gx * gx; sT[PS + e] = gx * gy; sT[2 * PS + e] = gx * gzv;
+                        sT[3 * PS + e] = gy * gy; sT[4 * PS + e] = gy * gzv; sT[5 * PS + e] = gzv * gzv;
                     }
-                    float2 gzv = __ffma2_rn(f2(wz.x), zu, __ffma2_rn(f2(wz.y), m, __fmul2_rn(f2(wz.z), zd)));
-                    if (!inner) {   // columns outside the volume: no gradient
-                        const int gxp = ox0 - a.off + pxc, gyp = oy0 - a.off + py;
-                        const bool ya = (unsigned)gyp < (unsigned)a.s1;
-                        gzv.x = (ya && (unsigned)gxp < (unsigned)a.s2) ? gzv.x : 0.0f;
-                        gzv.y = (ya && (unsigned)(gxp + 1) < (unsigned)a.s2) ? gzv.y : 0.0f;
-                        gy.x = (unsigned)gxp < (unsigned)a.s2 ? gy.x : 0.0f;
-                        gy.y = (unsigned)(gxp + 1) < (unsigned)a.s2 ? gy.y : 0.0f;
+                }
+            } else {
+#pragma unroll
+                for (int q = 0; q < NP; ++q) {
+                    const int e = tid + q * NT;
+                    if (e < PS) {
+                        const int ry = e / EX, rx = e - ry * EX;
+                        const int gxp = ix0 + rx, gyp = iy0 + ry;
+                        float gx = 0.0f, gy = 0.0f, gzv = 0.0f;
+                        if ((unsigned)gxp < (unsigned)a.s2 && (unsigned)gyp < (unsigned)a.s1) {
+                            const int c = (ry + 1) * RX + rx + 1;
+                            gx = grad2(R1[c - 1], R1[c], R1[c + 1], gxp, a.s2);
+                            gy = grad2(R1[c - RX], R1[c], R1[c + RX], gyp, a.s1);
+                            gzv = grad2(R0[c], R1[c], R2[c], iz, a.s0);
+                        }
+                        sT[e] = gx * gx; sT[PS + e] = gx * gy; sT[2 * PS + e] = gx * gzv;
+                        sT[3 * PS + e] = gy * gy; sT[4 * PS + e] = gy * gzv; sT[5 * PS + e] = gzv * gzv;
                     }
-                    float2* o = reinterpret_cast<float2*>(sT + py * G::SP + 2 * j);
-                    constexpr int PS2 = G::EY * G::SP / 2;             // channel stride in float2
-                    o[0] = __fmul2_rn(gx, gx);
-                    o[PS2] = __fmul2_rn(gx, gy);
-                    o[2 * PS2] = __fmul2_rn(gx, gzv);
-                    o[3 * PS2] = __fmul2_rn(gy, gy);
-                    o[4 * PS2] = __fmul2_rn(gy, gzv);
-                    o[5 * PS2] = __fmul2_rn(gzv, gzv);
                 }
             }
         }
-        if (__syncthreads_or(timed_out)) { qfail = q; break; }   // products ready; raw plane q - 1 no longer read
-        const bool zin = wz.x != 0.0f || wz.y != 0.0f || wz.z != 0.0f;
-        // ---- y blur: (channel, column pair, 4 output rows) per thread
-        for (int t = tid; zin && t < 6 * G::NPJ * 2; t += STX * STY) {
-            const int rh = t & 1, jj = (t >> 1) % G::NPJ, ch = (t >> 1) / G::NPJ;
-            const float2* col = reinterpret_cast<const float2*>(sT + ch * G::EY * G::SP + 4 * rh * G::SP + 2 * jj);
-            float2 v[K + 3];
+        // products ready; raw plane iz - 1 no longer read.  A wait that ran out ends the loop here, for all threads
+        if (__syncthreads_or(timed_out)) { qfail = qz; break; }
+        if (zin) {
+            for (int it = tid; it < 6 * EX; it += NT) {
+                const int c = it / EX, rx = it - c * EX;
+                const float* col = sT + c * PS + rx;
+                float cv[EY];
 #pragma unroll
-            for (int i = 0; i < K + 3; ++i) v[i] = col[i * (G::SP / 2)];
-            float2* dst = reinterpret_cast<float2*>(sY + ch * STY * G::SP + 4 * rh * G::SP + 2 * jj);
+                for (int r = 0; r < EY; ++r) cv[r] = col[r * EX];
 #pragma unroll
-            for (int o = 0; o < 4; ++o) {
-                float2 s2 = make_float2(0.0f, 0.0f);
+                for (int t = 0; t < STY; ++t) {
+                    float s = 0.0f;
 #pragma unroll
-                for (int k = 0; k < K; ++k) s2 = __ffma2_rn(a.g2[k], v[o + k], s2);
-                dst[o * (G::SP / 2)] = s2;
+                    for (int k = 0; k < K; ++k) s = fmaf(gw[k], cv[t + k], s);
+                    sY[(c * STY + t) * EX + rx] = s;
+                }
             }
         }
         __syncthreads();   // y blur ready
-        // ---- x blur of (x0, x0 + 1) for channels 3h .. 3h + 2, then the z window
-        float2 v[3];
+        float v[6];
         if (zin) {
 #pragma unroll
             for (int cc = 0; cc < 3; ++cc) {
-                const float2* row = reinterpret_cast<const float2*>(sY + ((3 * h + cc) * STY + ty) * G::SP + px);
-                float2 w[(K + 3) / 2];
+                const float2* row = reinterpret_cast<const float2*>(sY + ((3 * h + cc) * STY + ty) * EX + px);
+                float s0 = 0.0f, s1 = 0.0f;
 #pragma unroll
-                for (int i = 0; i < (K + 3) / 2; ++i) w[i] = row[i];
-                // value e of the row segment: e even -> w[e/2].x, odd -> w[e/2].y; outputs read e = k + p0 (+1)
-                float2 s2 = make_float2(0.0f, 0.0f);
-                if (p0 == 0) {
-#pragma unroll
-                    for (int k = 0; k < K; ++k) {
-                        if ((k & 1) == 0) s2 = __ffma2_rn(a.g2[k], w[k / 2], s2);
-                        else { s2.x = fmaf(a.g[k], w[k / 2].y, s2.x); s2.y = fmaf(a.g[k], w[k / 2 + 1].x, s2.y); }
-                    }
-                } else {
-#pragma unroll
-                    for (int k = 0; k < K; ++k) {
-                        if ((k & 1) == 1) s2 = __ffma2_rn(a.g2[k], w[(k + 1) / 2], s2);
-                        else { s2.x = fmaf(a.g[k], w[k / 2].y, s2.x); s2.y = fmaf(a.g[k], w[k / 2 + 1].x, s2.y); }
-                    }
+                for (int q = 0; q < (K + 1) / 2; ++q) {
+                    const float2 u = row[q];
+                    // u.x = sY[px + 2q], u.y = sY[px + 2q + 1]
+                    if (2 * q < K) s0 = fmaf(gw[2 * q], u.x, s0);
+                    if (2 * q + 1 < K) s0 = fmaf(gw[2 * q + 1], u.y, s0);
+                    if (2 * q >= 1) s1 = fmaf(gw[2 * q - 1], u.x, s1);
+                    s1 = fmaf(gw[2 * q], u.y, s1);
                 }
-                v[cc] = s2;
+                v[2 * cc] = s0; v[2 * cc + 1] = s1;
             }
         } else {
 #pragma unroll
-            for (int cc = 0; cc < 3; ++cc) v[cc] = make_float2(0.0f, 0.0f);
+            for (int o = 0; o < 6; ++o) v[o] = 0.0f;
         }
-        // z window: plane iz feeds the K outputs oz = iz + off - m, m = 0 .. K - 1; slot (iz - iz_lo) % K
-        float2 done[3];
-        st_zdispatch2<K>((iz - iz_lo) % K, acc, v, a.gz2, done);
+        float done[6];
+        st_zdispatch<K>((iz - iz_lo) % K, acc, v, gz, done);
+        // the slot just completed began at plane iz - K + 1: output oz
         const int oz = iz - (K - 1) + a.off;
-        if (oz >= oz_lo && y < a.o1 && x0 < a.o2) {
-            const size_t idx = (size_t(oz) * a.o1 + y) * a.o2 + x0;
-            const bool two = x0 + 1 < a.o2;
+        if (oz >= oz_lo && y < a.o1) {
+            const size_t row0 = (size_t(oz) * a.o1 + y) * a.o2;
 #pragma unroll
-            for (int cc = 0; cc < 3; ++cc) {
-                const int ch = 3 * h + cc;
+            for (int u = 0; u < 2; ++u) {
+                const int x = x0 + u;
+                if (x >= a.o2) continue;
+                const size_t idx = row0 + x;
+                const float c0 = done[u], c1 = done[2 + u], c2 = done[4 + u];   // channels 3h, 3h+1, 3h+2
                 if (a.layout == TVGB_LAYOUT_SYM6_PLANES) {
-                    float* o = a.out + size_t(ch) * on + idx;
-                    if (two && (reinterpret_cast<uintptr_t>(o) & 7) == 0) *reinterpret_cast<float2*>(o) = done[cc];
-                    else { o[0] = done[cc].x; if (two) o[1] = done[cc].y; }
+                    a.out[(3 * h) * on + idx] = c0; a.out[(3 * h + 1) * on + idx] = c1; a.out[(3 * h + 2) * on + idx] = c2;
                 } else if (a.layout == TVGB_LAYOUT_SYM6) {
-                    a.out[idx * 6 + ch] = done[cc].x;
-                    if (two) a.out[(idx + 1) * 6 + ch] = done[cc].y;
+                    float* o = a.out + idx * 6 + 3 * h;
+                    o[0] = c0; o[1] = c1; o[2] = c2;
                 } else {
-                    static constexpr int m9a[6] = {0, 1, 2, 4, 5, 8}, m9b[6] = {0, 3, 6, 4, 7, 8};
                     float* o = a.out + idx * 9;
-                    o[m9a[ch]] = done[cc].x; o[m9b[ch]] = done[cc].x;
-                    if (two) { o[9 + m9a[ch]] = done[cc].y; o[9 + m9b[ch]] = done[cc].y; }
+                    if (h == 0) { o[0] = c0; o[1] = c1; o[3] = c1; o[2] = c2; o[6] = c2; }
+                    else { o[4] = c0; o[5] = c1; o[7] = c1; o[8] = c2; }
                 }
             }
         }
     }
     if (qfail >= 0 && tid == 0) {
-        // a wait gave up (every thread left the loop at the same barrier): the planes from q + 1 on may still
-        // be in flight; wait for them (each slot holds at most one of them) before the shared memory is released
+        // the planes from qfail + 1 on may still be in flight (each slot holds at most one of them): wait for them
+        // before the shared memory is released
         atomicAdd(&g_st3_faults, 1u);
         for (int q = qfail + 1; q <= issued; ++q)
             tc::mbar_wait(&bars[q % ST_TMA_SLOTS], uint32_t(q / ST_TMA_SLOTS) & 1u, ST_TMA_WAIT_LIMIT);
@@ -727,10 +654,6 @@ int structure_tensor3_device(const float* vol, unsigned s0, unsigned s1, unsigne
     a.o0 = int(d[0]); a.o1 = int(d[1]); a.o2 = int(d[2]);
     a.K = int(K); a.off = mode == 0 ? 0 : int(K / 2);
     gaussian1d(K, sigma, a.g);
-    for (unsigned k = 0; k < K && k < 13; ++k) {
-        a.g2[k] = make_float2(a.g[k], a.g[k]);
-        a.gz2[k] = make_float2(0.25f * a.g[k], 0.25f * a.g[k]);
-    }
     a.out = out; a.layout = out_layout;
     const unsigned gx = ceil_div(d[2], STX), gy = ceil_div(d[1], STY);
     const bool fixed = K <= unsigned(ST_MAXT);
@@ -744,23 +667,23 @@ int structure_tensor3_device(const float* vol, unsigned s0, unsigned s1, unsigne
     size_t tma_smem = 0;
     const void* tfn = nullptr;
     switch (K) {
-        case 3: tfn = (const void*)k_st3t<3>; tma_smem = St3Geom<3>::SMEM; break;
-        case 5: tfn = (const void*)k_st3t<5>; tma_smem = St3Geom<5>::SMEM; break;
-        case 7: tfn = (const void*)k_st3t<7>; tma_smem = St3Geom<7>::SMEM; break;
-        case 9: tfn = (const void*)k_st3t<9>; tma_smem = St3Geom<9>::SMEM; break;
-        case 11: tfn = (const void*)k_st3t<11>; tma_smem = St3Geom<11>::SMEM; break;
-        case 13: tfn = (const void*)k_st3t<13>; tma_smem = St3Geom<13>::SMEM; break;
+        case 3: tfn = (const void*)k_st3_tma<3>; tma_smem = St3TmaGeom<3>::SMEM; break;
+        case 5: tfn = (const void*)k_st3_tma<5>; tma_smem = St3TmaGeom<5>::SMEM; break;
+        case 7: tfn = (const void*)k_st3_tma<7>; tma_smem = St3TmaGeom<7>::SMEM; break;
+        case 9: tfn = (const void*)k_st3_tma<9>; tma_smem = St3TmaGeom<9>::SMEM; break;
+        case 11: tfn = (const void*)k_st3_tma<11>; tma_smem = St3TmaGeom<11>::SMEM; break;
+        case 13: tfn = (const void*)k_st3_tma<13>; tma_smem = St3TmaGeom<13>::SMEM; break;
         default: break;
     }
     if (tfn && s2 % 4 == 0) {
         unsigned bx = 0, by = 0;
         switch (K) {
-            case 3: bx = St3Geom<3>::BX; by = St3Geom<3>::BY; break;
-            case 5: bx = St3Geom<5>::BX; by = St3Geom<5>::BY; break;
-            case 7: bx = St3Geom<7>::BX; by = St3Geom<7>::BY; break;
-            case 9: bx = St3Geom<9>::BX; by = St3Geom<9>::BY; break;
-            case 11: bx = St3Geom<11>::BX; by = St3Geom<11>::BY; break;
-            case 13: bx = St3Geom<13>::BX; by = St3Geom<13>::BY; break;
+            case 3: bx = St3TmaGeom<3>::BX; by = St3TmaGeom<3>::BY; break;
+            case 5: bx = St3TmaGeom<5>::BX; by = St3TmaGeom<5>::BY; break;
+            case 7: bx = St3TmaGeom<7>::BX; by = St3TmaGeom<7>::BY; break;
+            case 9: bx = St3TmaGeom<9>::BX; by = St3TmaGeom<9>::BY; break;
+            case 11: bx = St3TmaGeom<11>::BX; by = St3TmaGeom<11>::BY; break;
+            case 13: bx = St3TmaGeom<13>::BX; by = St3TmaGeom<13>::BY; break;
             default: break;
         }
         tma = make_tmap_3d_f32(&vmap, vol, s2, s1, s0, bx, by);
