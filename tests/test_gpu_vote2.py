@@ -79,3 +79,16 @@ def test_tk_ragged_sizes_against_oracle(mods):
         out = tk.tensorvote_tk(F, 3.0, 0.5, 2, 0, True, True, 20)
         ref = O.tensorvote2(F, 3.0, 0.5, 2, 19, samples=20)
         assert rel(out, ref) < 1e-4
+
+
+def test_tk_large_images_against_oracle(mods):
+    """The staged kernel on images of many CTAs (640 x 800 at power 2,
+    1024 x 960 at power 1), against the oracle."""
+    tk, _, _ = mods
+    rng = np.random.default_rng(7)
+    for (H, W), p in [((800, 640), 2), ((960, 1024), 1)]:
+        A = rng.normal(size=(H, W, 2, 2)).astype(np.float32)
+        F = (A @ np.swapaxes(A, -1, -2)).reshape(H, W, 4).astype(np.float32)
+        out = tk.tensorvote_tk(F, 3.0, 0.0, p, 0, True, True, 20)
+        ref = O.tensorvote2(F, 3.0, 0.0, p, 19, samples=20)
+        assert rel(out, ref) < 1e-4, (H, W, p)

@@ -145,22 +145,40 @@ __global__ void __launch_bounds__(V2X * V2Y) k_vote2_tk(const float4* __restrict
     if (x < s1 && y < s0) out[size_t(y) * s1 + x] = make_float4(sa + pa, sb + pb, sb + pb, sc + pc);
 }
 
-// Staged variant for windows whose voter tile fits in shared memory: the
-// CTA's 32 x 32 receivers (4 rows per thread) read their voters from a
-// (32 + 2 h) x (32 + 2 h) tile staged once, zero outside the image, so the
-// table loop has no bounds checks and each table entry (a warp-uniform
-// broadcast) serves 4 receivers.  h bounds |du|, |dv| over the table.
-template <int V2R, bool STICK, bool PLATE, bool P1>
-__global__ void __launch_bounds__(V2X * V2Y) k_vote2_tks(const float4* __restrict__ V, const Nb2* __restrict__ nb,
-                                                          int nbc, int s0, int s1, int h, float eta_s, unsigned power,
-                                                          float4* __restrict__ out) {
+// Staged variant for windows whose voter tile fits in shared memory: a CTA
+// of 32 x TY threads owns 32 x (TY V2R) receivers (V2R rows per thread, TY
+// apart) and reads their voters from a (32 + 2 h) x (TY V2R + 2 h) tile
+// staged once, zero outside the image, so the table loop has no bounds checks
+// and each table entry (a warp-uniform broadcast) serves V2R receivers.  h
+// bounds |du|, |dv| over the table.  The table streams through shared memory
+// in chunks of NBC entries.  Measured at 512^2 (C1, 20-step bench): TY = 8
+// (256 CTAs, 0.56 of a wave) 0.083 ms, TY = 4 0.092 ms, TY = 2 (1024 CTAs,
+// all resident) 0.094 ms: the kernel runs at the pace its warps' dependent
+// chains allow, and smaller CTAs buy no more warps per SM.
+//
+// Per pair, FP32 operations (the pipe that bounds the kernel): the stick
+// weight D = c1 (1 - q^2)^p + c2 (q^2)^p is, for p = 1, c1 + (c2 - c1) q^2
+// (one FMA with c2 - c1 formed once per entry); the reflected orientation
+// R q = q - 2 (q.d) d costs a multiply and two FMAs instead of the four
+// operations of the entry's (Ra, Rb, Rc) matrix product.  16 operations per
+// pair with the plate, against 19 for the reference's literal expressions;
+// both agree to FP32 rounding (0.092 -> 0.083 ms at C1).  A packed form
+// (two receiver rows per FFMA2 from a paired-row tile, pre-broadcast table
+// entries) measured 0.092 ms: a packed instruction holds the FP32 pipe as
+// long as two scalar ones, and its larger tile and entry loads cost more than
+// the issue slots it saves.
+template <int V2R, int TY, int NBC, bool STICK, bool PLATE, bool P1>
+__global__ void __launch_bounds__(V2X * TY) k_vote2_tks(const float4* __restrict__ V, const Nb2* __restrict__ nb,
+                                                        int nbc, int s0, int s1, int h, float eta_s, unsigned power,
+                                                        float4* __restrict__ out) {
     extern __shared__ __align__(16) float4 sm2[];
-    Nb2* snb = reinterpret_cast<Nb2*>(sm2);                       // NB_CHUNK entries
-    float4* tile = sm2 + NB_CHUNK * sizeof(Nb2) / sizeof(float4);  // TW x TW voters
-    const int TW = V2X + 2 * h;
-    const int x0 = blockIdx.x * V2X, y0 = blockIdx.y * (V2Y * V2R);
+    Nb2* snb = reinterpret_cast<Nb2*>(sm2);                       // NBC entries
+    float4* tile = sm2 + NBC * sizeof(Nb2) / sizeof(float4);      // TW x TH voters
+    constexpr int NT = V2X * TY;
+    const int TW = V2X + 2 * h, TH = TY * V2R + 2 * h;
+    const int x0 = blockIdx.x * V2X, y0 = blockIdx.y * (TY * V2R);
     const int tid = threadIdx.y * V2X + threadIdx.x;
-    for (int e = tid; e < TW * TW; e += V2X * V2Y) {
+    for (int e = tid; e < TW * TH; e += NT) {
         const int r = e / TW, c = e - r * TW;
         const int gy = y0 - h + r, gx = x0 - h + c;
         tile[e] = ((unsigned)gy < (unsigned)s0 && (unsigned)gx < (unsigned)s1) ? __ldg(V + size_t(gy) * s1 + gx)
@@ -169,32 +187,34 @@ __global__ void __launch_bounds__(V2X * V2Y) k_vote2_tks(const float4* __restric
     float sa[V2R], sb[V2R], sc[V2R], pa[V2R], pb[V2R], pc[V2R];
 #pragma unroll
     for (int j = 0; j < V2R; ++j) { sa[j] = sb[j] = sc[j] = pa[j] = pb[j] = pc[j] = 0.0f; }
-    // receiver j of this thread: (x0 + tx, y0 + ty + 8 j); its voter at (du, dv) is tile[ty + 8 j + h + dv][tx + h + du]
+    // receiver j of this thread: (x0 + tx, y0 + ty + TY j); its voter at (du, dv) is tile[ty + TY j + h + dv][tx + h + du]
     const float4* base = tile + (threadIdx.y + h) * TW + threadIdx.x + h;
-    for (int c0 = 0; c0 < nbc; c0 += NB_CHUNK) {
-        const int cn = min(NB_CHUNK, nbc - c0);
+    for (int c0 = 0; c0 < nbc; c0 += NBC) {
+        const int cn = min(NBC, nbc - c0);
         __syncthreads();
-        for (int i = tid; i < cn; i += V2X * V2Y) snb[i] = nb[c0 + i];
+        for (int i = tid; i < cn; i += NT) snb[i] = nb[c0 + i];
         __syncthreads();
 #pragma unroll 2
         for (int k = 0; k < cn; ++k) {
             const Nb2& e = snb[k];
             const float4* vp = base + e.dv * TW + e.du;
+            const float dc = e.c2 - e.c1;
 #pragma unroll
             for (int j = 0; j < V2R; ++j) {
-                const float4 v = vp[j * V2Y * TW];
+                const float4 v = vp[j * TY * TW];
                 if (STICK) {
                     const float qTd = fmaf(v.x, e.dx, v.y * e.dy);
                     const float q2 = qTd * qTd;
                     float D;
-                    if (P1) D = fmaf(e.c1, 1.0f - q2, e.c2 * q2);
+                    if (P1) D = fmaf(dc, q2, e.c1);
                     else {
                         const float t1 = 1.0f - q2, t2 = q2;
                         float e1 = t1, e2 = t2;
                         for (unsigned i = 1; i < power; ++i) { e1 *= t1; e2 *= t2; }
                         D = e.c1 * e1 + e.c2 * e2;
                     }
-                    const float Rqx = fmaf(e.Ra, v.x, e.Rb * v.y), Rqy = fmaf(e.Rb, v.x, e.Rc * v.y);
+                    const float k2 = -2.0f * qTd;
+                    const float Rqx = fmaf(k2, e.dx, v.x), Rqy = fmaf(k2, e.dy, v.y);
                     const float f = D * v.z;
                     const float fx = f * Rqx;
                     sa[j] = fmaf(fx, Rqx, sa[j]); sb[j] = fmaf(fx, Rqy, sb[j]); sc[j] = fmaf(f * Rqy, Rqy, sc[j]);
@@ -209,7 +229,7 @@ __global__ void __launch_bounds__(V2X * V2Y) k_vote2_tks(const float4* __restric
     if (x >= s1) return;
 #pragma unroll
     for (int j = 0; j < V2R; ++j) {
-        const int y = y0 + threadIdx.y + V2Y * j;
+        const int y = y0 + threadIdx.y + TY * j;
         if (y >= s0) break;
         const float a = fmaf(eta_s, sa[j], pa[j]), b = fmaf(eta_s, sb[j], pb[j]), c = fmaf(eta_s, sc[j], pc[j]);
         out[size_t(y) * s1 + x] = make_float4(a, b, b, c);
@@ -343,34 +363,22 @@ static int vote2_tk_launch(const float4* V, const Nb2* host_or_dev_nb, int nbc, 
         h = 0;
         for (int i = 0; i < nbc; ++i) h = std::max(h, std::max(std::abs(nbp[i].du), std::abs(nbp[i].dv)));
     }
-    const size_t tw = size_t(V2X) + 2 * size_t(h < 0 ? 0 : h);
-    const size_t smem_s = NB_CHUNK * sizeof(Nb2) + tw * tw * sizeof(float4);
+    // staged kernel: 4 receivers per thread (each table entry serves 4), 32 x 8 threads per CTA
+    constexpr int V2R = 4, TY = 8, V2NBC = 128;
+    const size_t hh = size_t(h < 0 ? 0 : h);
+    const size_t smem_s = V2NBC * sizeof(Nb2) + (V2X + 2 * hh) * (size_t(TY) * V2R + 2 * hh) * sizeof(float4);
     dim3 grid(ceil_div(S1, V2X), ceil_div(S0, V2Y)), blk(V2X, V2Y);
     {
         KernelTimer kt_("k_vote2_tk", st);
         if (h >= 0 && smem_s <= 200 * 1024) {
-            // receivers per thread: 4 (each table entry serves 4 receivers) measured fastest
-            // even where it leaves the GPU under one wave (512^2: 0.095 ms vs 0.117 / 0.133 ms
-            // for 2 / 1)
-#ifdef TVGB_V2R
-            const int R = TVGB_V2R;
-#else
-            const int R = 4;
-#endif
             const void* fn = nullptr;
-#define TVGB_TKS(RR)                                                                                          \
-    if (R == RR) {                                                                                              \
-        if (stick && use_plate) fn = p == 1 ? (const void*)k_vote2_tks<RR, true, true, true>                   \
-                                            : (const void*)k_vote2_tks<RR, true, true, false>;                 \
-        else if (stick) fn = p == 1 ? (const void*)k_vote2_tks<RR, true, false, true>                          \
-                                    : (const void*)k_vote2_tks<RR, true, false, false>;                        \
-        else fn = (const void*)k_vote2_tks<RR, false, true, true>;                                             \
-    }
-            TVGB_TKS(1) TVGB_TKS(2) TVGB_TKS(4)
-#undef TVGB_TKS
-            TVGB_CHECK_ARG(fn, "2D vote: no kernel for %d receivers per thread", R);
+            if (stick && use_plate) fn = p == 1 ? (const void*)k_vote2_tks<V2R, TY, V2NBC, true, true, true>
+                                                : (const void*)k_vote2_tks<V2R, TY, V2NBC, true, true, false>;
+            else if (stick) fn = p == 1 ? (const void*)k_vote2_tks<V2R, TY, V2NBC, true, false, true>
+                                        : (const void*)k_vote2_tks<V2R, TY, V2NBC, true, false, false>;
+            else fn = (const void*)k_vote2_tks<V2R, TY, V2NBC, false, true, true>;
             TVGB_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem_s)));
-            dim3 gs(ceil_div(S1, V2X), ceil_div(S0, unsigned(V2Y * R)));
+            dim3 gs(ceil_div(S1, V2X), ceil_div(S0, unsigned(TY * V2R))), bs(V2X, TY);
             const float4* vp = V;
             const Nb2* tp = dnb.get<Nb2>();
             int nbc_ = nbc, s0_ = int(S0), s1_ = int(S1), h_ = h;
@@ -378,7 +386,7 @@ static int vote2_tk_launch(const float4* V, const Nb2* host_or_dev_nb, int nbc, 
             unsigned p_ = p;
             float4* op = out;
             void* args[] = {&vp, &tp, &nbc_, &s0_, &s1_, &h_, &eta_, &p_, &op};
-            TVGB_CUDA(cudaLaunchKernel(fn, gs, blk, args, smem_s, st));
+            TVGB_CUDA(cudaLaunchKernel(fn, gs, bs, args, smem_s, st));
         } else if (stick && use_plate) {
             k_vote2_tk<true, true><<<grid, blk, 0, st>>>(V, dnb.get<Nb2>(), nbc, int(S0), int(S1), eta_s, p, out);
         } else if (stick) {
