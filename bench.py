@@ -617,7 +617,7 @@ def surrogate_study(vol_d, cfg, args, dev):
     the exact closed form, in the same kernel skeleton, on a bounded interior
     block of the benchmark's own field (the structure tensor of the whole
     volume, cropped): stick exact in every mode, plate by the rule named.
-    The network (7 -> 64 -> 64 -> 64 -> 6, BF16 on tcgen05) is trained first,
+    The network (28 features -> 64 -> 64 -> 64 -> 6, BF16 on tcgen05) is trained first,
     on the GPU, on 2^24 samples of the plain integral.  Errors are against
     the closed form, the exact integral (within 2e-6 of the FP64 oracle)."""
     import ctypes
@@ -675,7 +675,8 @@ def surrogate_study(vol_d, cfg, args, dev):
     return {
         "sample": f"{b}^3 interior block of this field (structure tensor of the whole volume, cropped), sigma "
                   f"{cfg['sigma']:g}, w {cfg['w']}; stick exact, plate by the rule named; ball off",
-        "network": f"7-64-64-64-6 GELU, BF16 weights and activations, FP32 accumulation, tcgen05.mma with the "
+        "network": f"28-64-64-64-6 GELU (inputs: direction, normal, flag and their degree-2 monomials), BF16 "
+                   f"weights and activations, FP32 accumulation, tcgen05.mma with the "
                    f"activations in tensor memory; trained here on 2^24 plain-integral samples, {args.sur_steps} "
                    f"Adam steps of 8192 (lr {args.sur_lr:g}, cosine decay)",
         "train_s": t_train, "final_loss": float(np.mean(hist[-100:])), "heldout_rel_err": heldout,
@@ -1107,8 +1108,8 @@ def main():
     ap.add_argument("--sur-modes", default="", help="comma-separated subset of the surrogate study's modes "
                                                     "(plain64, surrogate_judged, surrogate_judged_1e-2, "
                                                     "surrogate_unjudged); the exact vote always runs")
-    ap.add_argument("--sur-steps", type=int, default=100000, help="Adam steps of the surrogate's training")
-    ap.add_argument("--sur-lr", type=float, default=6e-3, help="peak learning rate of the surrogate's training")
+    ap.add_argument("--sur-steps", type=int, default=300000, help="Adam steps of the surrogate's training")
+    ap.add_argument("--sur-lr", type=float, default=3e-3, help="peak learning rate of the surrogate's training")
     ap.add_argument("--config", choices=["c2", "c4", "c5", "c3", "c1"], default="c4",
                     help="c4: 3D pipeline at 384^3, sigma 4, the surrogate study's field (the headline); c2: the same "
                          "at 256^3; c5: 512^3 tubes + sheets, sigma 6, stick + plate + ball (capacity); c3: batched "

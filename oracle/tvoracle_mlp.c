@@ -1,18 +1,19 @@
 /* CPU FP64 restatement of the plate / ball vote surrogate: the MLP
- * 7 -> 64 -> 64 -> 64 -> 6 (GELU, tanh form) and its backward pass, and the
- * "plain orientation integral" the surrogate is trained on.  Test
- * infrastructure: the GPU training kernels' gradients and the GPU sample
- * generator are checked against these.
+ * 28 -> 64 -> 64 -> 64 -> 6 (GELU, tanh form) over the 28 features of the
+ * raw input (d, n, flag) -- the input itself, d_i d_j and n_i n_j (i <= j),
+ * d_i n_j -- and its backward pass, and the "plain orientation integral" the
+ * surrogate is trained on.  Test infrastructure: the GPU training kernels'
+ * gradients and the GPU sample generator are checked against these.
  *
  * Parameter layout (float64 here, float32 master copy on the GPU), padded to
- * 8 inputs / 8 outputs with zero rows / columns:
- *   W1[64][8] b1[64] W2[64][64] b2[64] W3[64][64] b3[64] W4[8][64] b4[8]
+ * 8 outputs with zero rows:
+ *   W1[64][28] b1[64] W2[64][64] b2[64] W3[64][64] b3[64] W4[8][64] b4[8]
  * Quantised forward (quant != 0): weights and each hidden layer's input
- * rounded to bfloat16 (round to nearest even of the float32 value), the
- * network's inputs taken as bf16(x) + bf16(x - bf16(x)) (the tensor-core
- * form feeds each input and its residual against the same weight), as the
- * tensor-core inference computes; the backward pass treats the rounding as
- * identity.
+ * rounded to bfloat16 (round to nearest even of the float32 value), each
+ * feature formed in float32 (a product rounded once) and taken as
+ * bf16(f) + bf16(f - bf16(f)) (the tensor-core form feeds each feature and
+ * its residual against the same weight), as the tensor-core inference
+ * computes; the backward pass treats the rounding as identity.
  * quant == 1: GELU exact, then rounded to bfloat16 (the GPU's FP32 GELU);
  * quant == 2: the activation as the GPU's training forward pass and its
  * tcgen05 inference compute it: for units j with j % 8 < 6 the GELU in packed
@@ -28,7 +29,8 @@
 #include "tvoracle.h"
 
 #define PI_D 3.14159265358979323846
-#define MLP_IN 8
+#define MLP_IN 28
+#define MLP_X 8     /* floats per sample row of X (7 used) */
 #define MLP_H 64
 #define MLP_OUT 8
 
@@ -75,6 +77,23 @@ static double gelu_d(double z) {
     return 0.5 * (1.0 + t) + 0.5 * z * (1.0 - t * t) * GELU_K * (1.0 + 3.0 * GELU_A * z * z);
 }
 
+/* the 28 features of a raw input x = (d0, d1, d2, n0, n1, n2, flag); with
+ * quant, x is float32 and each product is rounded to float32 once */
+static void features(const double* x, int quant, double* f) {
+    const double* d = x;
+    const double* nv = x + 3;
+    int k = 0;
+    for (int i = 0; i < 7; ++i) f[k++] = quant ? (double)(float)x[i] : x[i];
+#define OR_PROD(a, b) (quant ? (double)((float)(a) * (float)(b)) : (a) * (b))
+    for (int i = 0; i < 3; ++i)
+        for (int j = i; j < 3; ++j) f[k++] = OR_PROD(d[i], d[j]);
+    for (int i = 0; i < 3; ++i)
+        for (int j = i; j < 3; ++j) f[k++] = OR_PROD(nv[i], nv[j]);
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) f[k++] = OR_PROD(d[i], nv[j]);
+#undef OR_PROD
+}
+
 int or_mlp_param_count(void) { return MLP_H * MLP_IN + MLP_H + 2 * (MLP_H * MLP_H + MLP_H) + MLP_OUT * MLP_H + MLP_OUT; }
 
 /* forward + backward over B samples (X: B x 8, T: B x 8 targets; only the
@@ -90,7 +109,7 @@ double or_mlp_loss_grad(const double* P, const double* X, const double* T, int B
     const double* W4 = b3 + MLP_H;
     const double* b4 = W4 + MLP_OUT * MLP_H;
     const int np = or_mlp_param_count();
-    double Wq[64 * 64 * 2 + 64 * 8 * 2];
+    double Wq[MLP_H * MLP_IN + 2 * MLP_H * MLP_H + MLP_OUT * MLP_H];
     double* W1q = Wq;
     double* W2q = W1q + MLP_H * MLP_IN;
     double* W3q = W2q + MLP_H * MLP_H;
@@ -110,11 +129,10 @@ double or_mlp_loss_grad(const double* P, const double* X, const double* T, int B
     double loss = 0.0;
     for (int s = 0; s < B; ++s) {
         double h0[MLP_IN], z1[MLP_H], h1[MLP_H], z2[MLP_H], h2[MLP_H], z3[MLP_H], h3[MLP_H];
-        /* quantised: each input as bf16(x) + bf16(x - bf16(x)), the network's first layer taking both */
-        for (int k = 0; k < MLP_IN; ++k) {
-            const double x = X[s * MLP_IN + k];
-            h0[k] = quant ? bf16r(x) + bf16r(x - bf16r(x)) : x;
-        }
+        /* quantised: each feature as bf16(f) + bf16(f - bf16(f)), the network's first layer taking both */
+        double f[MLP_IN];
+        features(X + s * MLP_X, quant, f);
+        for (int k = 0; k < MLP_IN; ++k) h0[k] = quant ? bf16r(f[k]) + bf16r(f[k] - bf16r(f[k])) : f[k];
         for (int j = 0; j < MLP_H; ++j) {
             double a = b1[j];
             for (int k = 0; k < MLP_IN; ++k) a += W1q[j * MLP_IN + k] * h0[k];

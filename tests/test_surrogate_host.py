@@ -46,9 +46,9 @@ def test_target_is_the_exact_plate_and_ball():
 def test_weights_file_roundtrip_and_checksum(tmp_path):
     from tiralib_gb300 import surrogate as S
     p = S.init_params(3)
-    assert p.size == S.param_count() == O.mlp_param_count()
-    W1 = p[:512].reshape(64, 8)
-    assert np.all(W1[:, 7] == 0)
+    assert p.size == S.param_count() == O.mlp_param_count() == 64 * 28 + 64 + 2 * (64 * 64 + 64) + 8 * 64 + 8
+    W4 = p[64 * 28 + 64 + 2 * (64 * 64 + 64):][:512].reshape(8, 64)
+    assert np.all(W4[6:] == 0) and np.any(W4[:6] != 0)
     f = os.path.join(tmp_path, "net.bin")
     S.save(f, p, "sigma2 = 0, power 1")
     q, note = S.load(f)

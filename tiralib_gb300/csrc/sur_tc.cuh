@@ -1,26 +1,27 @@
-// The surrogate's MLP (surrogate_mlp.cuh: 7 -> 64 -> 64 -> 64 -> 6, GELU,
-// BF16 weights and activations, FP32 accumulation) on the fifth-generation
-// tensor cores: tcgen05.mma with M = 128 rows (one (receiver, voter) pair or
-// one sample per row, one row per thread of a 128-thread CTA), the
-// activations in tensor memory (TMEM) as the A operand, the weights in shared
-// memory as the B operand.
+// The surrogate's MLP (surrogate_mlp.cuh: 28 features -> 64 -> 64 -> 64 -> 6,
+// GELU, BF16 weights and activations, FP32 accumulation) on the
+// fifth-generation tensor cores: tcgen05.mma with M = 128 rows (one
+// (receiver, voter) pair or one sample per row, one row per thread of a
+// 128-thread CTA), the activations in tensor memory (TMEM) as the A operand,
+// the weights in shared memory as the B operand.
 //
 // TMEM columns of the CTA's allocation (128):
 //   [0, 64)    D: the FP32 accumulator of the current layer (N = 64; the
 //              output layer uses [0, 16))
-//   [64, 96)   A: the current layer's input, BF16 pairs (64 values); the
-//              first layer's 16 inputs use [64, 72)
+//   [64, 96)   A: the current layer's input, BF16 pairs (64 values): layer
+//              1's row of 64 (sur_row64: features, the bias pair, residuals),
+//              then each hidden layer's activations
 //   [96, 104)  a constant block: (1, 1, 0, ..., 0) in BF16.  The weight image
-//              carries each bias as bf16(b) and bf16(b - bf16(b)) in the two
-//              K columns that meet it, so the MMA adds the bias in FP32 to
-//              ~2^-16 relative and no epilogue instruction is spent on it.
-// Layer 1 reads its 7 inputs, a 1 and a 1 (the bias pair), then the BF16
-// residuals of inputs 0..5 (meeting the same weights) from [64, 72).
+//              carries each hidden and output bias as bf16(b) and
+//              bf16(b - bf16(b)) in the two K columns that meet it, so the
+//              MMA adds the bias in FP32 to ~2^-16 relative and no epilogue
+//              instruction is spent on it.  (Layer 1's bias pair is part of
+//              its own row.)
 //
 // Weight image (shared memory, bytes), each matrix N x K, K-major, in 8 x 8
 // core matrices without swizzle (LBO = 128 B along K, SBO = (K / 8) * 128 B
-// along N):  B1 64 x 16 at 0, B2 64 x 80 at 2048, B3 64 x 80 at 12288,
-// B4 16 x 80 at 22528; 25088 bytes in all.
+// along N):  B1 64 x 64 at 0, B2 64 x 80 at 8192, B3 64 x 80 at 18432,
+// B4 16 x 80 at 28672; 31232 bytes in all.
 //
 // Where the time goes (GB300, measured): the three GELU epilogues per tile.
 // With every unit on the tanh form the MUFU pipe was 71% busy; with one unit
@@ -35,8 +36,8 @@ namespace tvgb {
 
 constexpr int TC_COLS = 128;                    // TMEM columns per CTA
 constexpr int TC_D = 0, TC_A = 64, TC_ONE = 96;
-constexpr int TC_B1 = 0, TC_B2 = 2048, TC_B3 = 12288, TC_B4 = 22528, TC_IMG_BYTES = 25088;
-constexpr int TC_K1 = 16, TC_KH = 80;           // K of layer 1 and of layers 2..4
+constexpr int TC_B1 = 0, TC_B2 = 8192, TC_B3 = 18432, TC_B4 = 28672, TC_IMG_BYTES = 31232;
+constexpr int TC_K1 = SUR_K1, TC_KH = 80;       // K of layer 1 and of layers 2..4
 constexpr uint32_t TC_WAIT_LIMIT = 1u << 24;    // mbarrier polls before a kernel gives up
 // dynamic shared memory requested per CTA: at most 4 CTAs (4 x TC_COLS = all
 // 512 TMEM columns) fit on an SM, so no CTA waits in tcgen05.alloc
@@ -148,8 +149,11 @@ __device__ __forceinline__ bool sur_tc_layer(SurTc& s) {
     if (threadIdx.x == 0) {
         tc::fence_after_sync();
         if (LAYER == 1) {
-            tc::mma_ts(s.tmem + TC_D, s.tmem + TC_A, tc::smem_desc(s.img + TC_B1, 128, 256),
-                       tc::idesc_bf16_f32(128, 64), 0u);
+            const uint32_t idesc = tc::idesc_bf16_f32(128, 64);
+#pragma unroll
+            for (int k = 0; k < TC_K1 / 16; ++k)
+                tc::mma_ts(s.tmem + TC_D, s.tmem + TC_A + 8 * k, tc::smem_desc(s.img + TC_B1 + 256 * k, 128, 1024),
+                           idesc, k > 0 ? 1u : 0u);
         } else {
             const uint32_t b = s.img + (LAYER == 2 ? TC_B2 : (LAYER == 3 ? TC_B3 : TC_B4));
             const uint32_t idesc = tc::idesc_bf16_f32(128, LAYER == 4 ? 16 : 64);
@@ -186,10 +190,9 @@ __device__ __forceinline__ void sur_tc_hidden(const SurTc& s) {
     tc::tmem_st32(t + TC_A, act);
 }
 
-// Layers 1..4 after the caller stored this thread's layer-1 input row into
-// TMEM (8 BF16 pairs at TC_A: x0..x6, then 1, 1 for the bias, then the
-// residuals x_k - bf16(x_k) of x0..x5, then a zero);
-// leaves the 16 output columns in D.  Returns false if a wait gave up.
+// Layers 1..4 after the caller stored this thread's layer-1 input row
+// (sur_row64: 32 BF16 pairs) into TMEM at TC_A; leaves the 16 output columns
+// in D.  Returns false if a wait gave up.
 template <int GM>
 __device__ __forceinline__ bool sur_tc_layers(SurTc& s) {
     if (!sur_tc_layer<1>(s)) return false;
@@ -202,11 +205,12 @@ __device__ __forceinline__ bool sur_tc_layers(SurTc& s) {
 }
 
 // One 128-row tile through the network: in = this thread's layer-1 input
-// row, out = its 8 output columns (6 used).  Returns false if a wait gave up.
+// row (sur_row64), out = its 8 output columns (6 used).  Returns false if a
+// wait gave up.
 template <int GM>
-__device__ __forceinline__ bool sur_tc_forward(SurTc& s, const uint32_t (&in)[8], float (&out)[8]) {
+__device__ __forceinline__ bool sur_tc_forward(SurTc& s, const uint32_t (&in)[SUR_K1 / 2], float (&out)[8]) {
     const uint32_t t = s.tmem + tc_lane_base();
-    if (!s.failed) tc::tmem_st8(t + TC_A, in);
+    if (!s.failed) tc::tmem_st32(t + TC_A, in);
     if (!sur_tc_layers<GM>(s) || s.failed) return false;
     uint32_t r[16];
     tc::tmem_ld16(t + TC_D, r);

@@ -32,14 +32,33 @@ static uint16_t bf16_bits(float f) {          // round to nearest even
     return uint16_t(u >> 16);
 }
 
+// a bias as the two BF16 values whose sum the MMA forms in FP32
+static void bias_split(float b, float& hi, float& lo) {
+    const uint32_t u = uint32_t(bf16_bits(b)) << 16;
+    std::memcpy(&hi, &u, 4);
+    lo = b - hi;
+}
+
+// layer 1's weight meeting K column k of the input row (sur_row64's layout):
+// W1 for a feature or its residual, the split b1 for the bias pair
+static float w1_at(const float* P, int j, int k) {
+    if (k < SUR_IN) return P[SUR_W1 + j * SUR_IN + k];
+    if (k == SUR_IN || k == SUR_IN + 1) {
+        float hi, lo;
+        bias_split(P[SUR_B1 + j], hi, lo);
+        return k == SUR_IN ? hi : lo;
+    }
+    if (k >= 32 && k < 32 + SUR_IN) return P[SUR_W1 + j * SUR_IN + (k - 32)];
+    return 0.0f;
+}
+
 void sur_make_fragments(const float* P, uint2* frag, float* bias) {
     struct L { int w, kin, nout, kt, nt, fbase; };
-    const L layers[4] = {{SUR_W1, SUR_IN, SUR_H, 1, 8, SUR_F1}, {SUR_W2, SUR_H, SUR_H, 4, 8, SUR_F2},
+    const L layers[4] = {{SUR_W1, SUR_K1, SUR_H, 4, 8, SUR_F1}, {SUR_W2, SUR_H, SUR_H, 4, 8, SUR_F2},
                          {SUR_W3, SUR_H, SUR_H, 4, 8, SUR_F3}, {SUR_W4, SUR_H, SUR_OUT, 4, 1, SUR_F4}};
     for (const L& l : layers) {
-        // layer 1: K columns 8..15 carry the inputs' BF16 residuals, with the same weights
         auto w = [&](int j, int k) {
-            if (l.fbase == SUR_F1 && k >= 8 && k < 8 + l.kin) k -= 8;
+            if (l.fbase == SUR_F1) return w1_at(P, j, k);
             return k < l.kin ? P[l.w + j * l.kin + k] : 0.0f;
         };
         for (int kt = 0; kt < l.kt; ++kt)
@@ -69,17 +88,14 @@ void sur_make_tc_image(const float* P, uint16_t* img) {
     };
     // a bias as the two BF16 values whose sum the MMA forms in FP32
     auto put_bias = [&](int base, int K, int n, int k, float b) {
-        const uint32_t u = uint32_t(bf16_bits(b)) << 16;
-        float hi;
-        std::memcpy(&hi, &u, 4);
-        put(base, K, n, k, b);
-        put(base, K, n, k + 1, b - hi);
+        float hi, lo;
+        bias_split(b, hi, lo);
+        put(base, K, n, k, hi);
+        put(base, K, n, k + 1, lo);
     };
     for (int n = 0; n < SUR_H; ++n) {
-        for (int k = 0; k < 7; ++k) put(TC_B1, TC_K1, n, k, P[SUR_W1 + n * SUR_IN + k]);
-        put_bias(TC_B1, TC_K1, n, 7, P[SUR_B1 + n]);
-        // K columns 9..14: the BF16 residuals of inputs 0..5 (direction and normal), same weights
-        for (int k = 0; k < 6; ++k) put(TC_B1, TC_K1, n, 9 + k, P[SUR_W1 + n * SUR_IN + k]);
+        // layer 1: features, the bias pair, the features' residuals (sur_row64's K layout)
+        for (int k = 0; k < TC_K1; ++k) put(TC_B1, TC_K1, n, k, w1_at(P, n, k));
         for (int k = 0; k < SUR_H; ++k) {
             put(TC_B2, TC_KH, n, k, P[SUR_W2 + n * SUR_H + k]);
             put(TC_B3, TC_KH, n, k, P[SUR_W3 + n * SUR_H + k]);
@@ -222,10 +238,13 @@ __global__ void __launch_bounds__(256) k_sur_fwd_bwd(const float* __restrict__ P
     for (int e = tid; e < SUR_H; e += 256) { S.b[e] = P[SUR_B1 + e]; S.b[SUR_H + e] = P[SUR_B2 + e]; S.b[2 * SUR_H + e] = P[SUR_B3 + e]; }
     if (tid < SUR_OUT) S.b[3 * SUR_H + tid] = P[SUR_B4 + tid];
     const size_t base = first + size_t(blockIdx.x) * TRB;
-    // each input as the first layer sees it: bf16(x) + bf16 of its residual
-    for (int e = tid; e < TRB * SUR_IN; e += 256) {
-        const float x = X[((base + e / SUR_IN) % n) * 8 + e % SUR_IN];
-        S.h0[e] = bq(x) + bq(bf16_residual(x));
+    // each feature as the first layer sees it: bf16(f) + bf16 of its residual
+    if (tid < TRB) {
+        const float* xs = X + ((base + tid) % n) * 8;
+        float x[SUR_X], f[SUR_IN];
+        for (int k = 0; k < SUR_X; ++k) x[k] = xs[k];
+        sur_features(x, f);
+        for (int k = 0; k < SUR_IN; ++k) S.h0[tid * SUR_IN + k] = bq(f[k]) + bq(bf16_residual(f[k]));
     }
     __syncthreads();
 
@@ -372,12 +391,23 @@ __global__ void __launch_bounds__(128) k_sur_eval(const uint2* __restrict__ frag
     const size_t warps = size_t(gridDim.x) * (blockDim.x >> 5);
     for (size_t tile = size_t(blockIdx.x) * (blockDim.x >> 5) + (threadIdx.x >> 5); tile * 16 < n; tile += warps) {
         const size_t r0 = tile * 16 + g, r1 = r0 + 8;
-        float x0[2] = {0, 0}, x1[2] = {0, 0};
-        if (r0 < n) { x0[0] = X[r0 * 8 + 2 * t]; x0[1] = X[r0 * 8 + 2 * t + 1]; }
-        if (r1 < n) { x1[0] = X[r1 * 8 + 2 * t]; x1[1] = X[r1 * 8 + 2 * t + 1]; }
-        const uint32_t a[4] = {pack_bf16x2(x0[0], x0[1]), pack_bf16x2(x1[0], x1[1]),
-                               pack_bf16x2(bf16_residual(x0[0]), bf16_residual(x0[1])),
-                               pack_bf16x2(bf16_residual(x1[0]), bf16_residual(x1[1]))};
+        float x0[SUR_X] = {0, 0, 0, 0, 0, 0, 0}, x1[SUR_X] = {0, 0, 0, 0, 0, 0, 0};
+        if (r0 < n) for (int k = 0; k < SUR_X; ++k) x0[k] = X[r0 * 8 + k];
+        if (r1 < n) for (int k = 0; k < SUR_X; ++k) x1[k] = X[r1 * 8 + k];
+        uint32_t row0[SUR_K1 / 2], row1[SUR_K1 / 2];
+        sur_row64(x0, row0);
+        sur_row64(x1, row1);
+        if (r0 >= n) for (int i = 0; i < SUR_K1 / 2; ++i) row0[i] = 0u;
+        if (r1 >= n) for (int i = 0; i < SUR_K1 / 2; ++i) row1[i] = 0u;
+        // A fragment of k-tile kt: rows g / g + 8, columns 16 kt + 2 t (pair 8 kt + t) and + 8 (pair 8 kt + 4 + t)
+        uint32_t a[4][4];
+#pragma unroll
+        for (int kt = 0; kt < 4; ++kt) {
+            a[kt][0] = row0[8 * kt + t];
+            a[kt][1] = row1[8 * kt + t];
+            a[kt][2] = row0[8 * kt + 4 + t];
+            a[kt][3] = row1[8 * kt + 4 + t];
+        }
         float out[4];
         sur_mlp16(frag, bias, a, out);
         if (r0 < n) { Y[r0 * 8 + 2 * t] = out[0]; Y[r0 * 8 + 2 * t + 1] = out[1]; }
@@ -403,12 +433,9 @@ __global__ void __launch_bounds__(128) k_sur_eval_tc(const uint4* __restrict__ i
             x0 = reinterpret_cast<const float4*>(X)[row * 2];
             x1 = reinterpret_cast<const float4*>(X)[row * 2 + 1];
         }
-        // inputs 0..6, the bias pair (1, 1), the residuals of inputs 0..5
-        const uint32_t in[8] = {pack_bf16x2(x0.x, x0.y), pack_bf16x2(x0.z, x0.w), pack_bf16x2(x1.x, x1.y),
-                                pack_bf16x2(x1.z, 1.0f), pack_bf16x2(1.0f, bf16_residual(x0.x)),
-                                pack_bf16x2(bf16_residual(x0.y), bf16_residual(x0.z)),
-                                pack_bf16x2(bf16_residual(x0.w), bf16_residual(x1.x)),
-                                pack_bf16x2(bf16_residual(x1.y), 0.0f)};
+        const float x[SUR_X] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z};
+        uint32_t in[SUR_K1 / 2];
+        sur_row64(x, in);
         float out[8];
         if (!sur_tc_forward<GM>(s, in, out)) break;
         if (row < n) {

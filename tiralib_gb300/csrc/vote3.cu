@@ -1789,14 +1789,11 @@ __global__ void __launch_bounds__(128) k_vote3_surtc(SurVoteArgs a) {
                     const float il = rsqrtf(float(L2));
                     float dv[3] = {oxf * il, oyf * il, ozf * il}, nv[3] = {B.x, B.y, B.z};
                     sur_canonical(dv, nv, true);
-                    // inputs, the bias pair, the inputs' BF16 residuals (sur_tc.cuh's layer-1 layout)
-                    const uint32_t in8[8] = {pack_bf16x2(dv[0], dv[1]), pack_bf16x2(dv[2], nv[0]),
-                                             pack_bf16x2(nv[1], nv[2]), pack_bf16x2(1.0f, 1.0f),
-                                             pack_bf16x2(1.0f, bf16_residual(dv[0])),
-                                             pack_bf16x2(bf16_residual(dv[1]), bf16_residual(dv[2])),
-                                             pack_bf16x2(bf16_residual(nv[0]), bf16_residual(nv[1])),
-                                             pack_bf16x2(bf16_residual(nv[2]), 0.0f)};
-                    if (!tcs.failed) tc::tmem_st8(tA, in8);
+                    // layer 1's row: the features, the bias pair, the features' BF16 residuals (sur_row64)
+                    const float xin[SUR_X] = {dv[0], dv[1], dv[2], nv[0], nv[1], nv[2], 1.0f};
+                    uint32_t row[SUR_K1 / 2];
+                    sur_row64(xin, row);
+                    if (!tcs.failed) tc::tmem_st32(tA, row);
                     if (!sur_tc_layer<1>(tcs)) { ok = false; break; }
                     // the exact stick vote while layer 1 runs
                     if (STICK)

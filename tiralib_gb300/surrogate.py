@@ -1,10 +1,13 @@
 """The learned plate / ball vote (MLP surrogate) on the GPU.
 
-The network, 7 -> 64 -> 64 -> 64 -> 6 with GELU, maps (offset direction
-o / |o|, plate normal n, flag: 1 plate / 0 ball) to the angular part of the
-unit-scale plate or ball vote at offset o (sigma2 = 0, power 1; the
-Gaussian exp(-|o|^2 / sigma^2) is applied analytically, so the direction
-is all the network needs).  Everything runs in libtvgb:
+The network, 28 -> 64 -> 64 -> 64 -> 6 with GELU, maps the features of
+(offset direction d = o / |o|, plate normal n, flag: 1 plate / 0 ball) --
+the seven inputs and the degree-2 monomials d_i d_j, n_i n_j, d_i n_j -- to
+the angular part of the unit-scale plate or ball vote at offset o
+(sigma2 = 0, power 1; the Gaussian exp(-|o|^2 / sigma^2) is applied
+analytically, so the direction is all the network needs).  Sample rows (X)
+hold the seven raw inputs (8 floats); the features are formed in the
+kernels.  Everything runs in libtvgb:
 
   samples(n, seed)          training pairs from the plain 64-orientation integral
   train(params, X, T, ...)  quantisation-aware training by its own kernels
@@ -29,6 +32,7 @@ PLATE_SURROGATE, PLATE_CLOSED, PLATE_PLAIN64 = 0, 1, 2
 _MODES = {"surrogate": PLATE_SURROGATE, "closed": PLATE_CLOSED, "plain64": PLATE_PLAIN64}
 
 _MAGIC = b"TVGBSUR1"
+_VERSION = 2          # 2: the 28-feature first layer (1: seven raw inputs)
 
 
 def param_count():
@@ -38,7 +42,7 @@ def param_count():
 def layout():
     """(name, offset, shape) of each parameter block in the flat vector."""
     out, off = [], 0
-    for name, shape in (("W1", (64, 8)), ("b1", (64,)), ("W2", (64, 64)), ("b2", (64,)), ("W3", (64, 64)),
+    for name, shape in (("W1", (64, 28)), ("b1", (64,)), ("W2", (64, 64)), ("b2", (64,)), ("W3", (64, 64)),
                         ("b3", (64,)), ("W4", (8, 64)), ("b4", (8,))):
         out.append((name, off, shape))
         off += int(np.prod(shape))
@@ -46,19 +50,15 @@ def layout():
 
 
 def init_params(seed=0):
-    """Glorot-uniform weights, zero biases; the padded input column and output
-    rows are zero."""
+    """Glorot-uniform weights, zero biases; the padded output rows are zero."""
     rng = np.random.default_rng(seed)
     p = np.zeros(param_count(), np.float32)
     for name, off, shape in layout():
         if name.startswith("W"):
             fan_out, fan_in = shape
-            fan_in = 7 if name == "W1" else fan_in
             fan_out = 6 if name == "W4" else fan_out
             lim = np.sqrt(6.0 / (fan_in + fan_out))
             w = rng.uniform(-lim, lim, shape).astype(np.float32)
-            if name == "W1":
-                w[:, 7] = 0.0
             if name == "W4":
                 w[6:, :] = 0.0
             p[off:off + w.size] = w.ravel()
@@ -172,7 +172,8 @@ def save(path, params, meta=""):
     payload = p.tobytes()
     note = meta.encode("utf-8")
     with open(path, "wb") as f:
-        f.write(_MAGIC + struct.pack("<III", 1, p.size, len(note)) + hashlib.sha256(payload).digest() + note + payload)
+        f.write(_MAGIC + struct.pack("<III", _VERSION, p.size, len(note)) + hashlib.sha256(payload).digest() + note
+                + payload)
 
 
 def load(path):
@@ -183,7 +184,7 @@ def load(path):
     if blob[:8] != _MAGIC:
         raise ValueError(f"{path}: not a surrogate weights file")
     version, count, nlen = struct.unpack("<III", blob[8:20])
-    if version != 1 or count != param_count():
+    if version != _VERSION or count != param_count():
         raise ValueError(f"{path}: unsupported version {version} or size {count}")
     digest = blob[20:52]
     note = blob[52:52 + nlen].decode("utf-8")
