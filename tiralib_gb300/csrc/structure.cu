@@ -70,6 +70,7 @@ struct StArgs {
     float g[MAXK];
     float* out;
     int layout;
+    int pair_store;       // planes layout, even o2, 8-byte aligned out: 64-bit stores of x pairs
 };
 
 // d/d(axis) at an in-volume voxel: volume<T>::gradient's rule
@@ -396,7 +397,17 @@ __global__ void __launch_bounds__(STX * STY, 2) k_st3(StArgs a) {
         st_zdispatch<K>((iz - iz_lo) % K, acc, v, gz, done);
         // the slot just completed began at plane iz - K + 1: output oz
         const int oz = iz - (K - 1) + a.off;
-        if (oz >= oz_lo && y < a.o1) {
+        if (oz >= oz_lo && y < a.o1 && a.pair_store) {
+            // planes, even row length, 8-byte aligned output: the thread's two x neighbours as one 64-bit store per
+            // channel (x0 even, so both are in the row or neither)
+            if (x0 < a.o2) {
+                float2* o = reinterpret_cast<float2*>(a.out + (3 * h) * on + (size_t(oz) * a.o1 + y) * a.o2 + x0);
+                const size_t on2 = on / 2;
+                o[0] = make_float2(done[0], done[1]);
+                o[on2] = make_float2(done[2], done[3]);
+                o[2 * on2] = make_float2(done[4], done[5]);
+            }
+        } else if (oz >= oz_lo && y < a.o1) {
             const size_t row0 = (size_t(oz) * a.o1 + y) * a.o2;
 #pragma unroll
             for (int u = 0; u < 2; ++u) {
@@ -600,7 +611,17 @@ __global__ void __launch_bounds__(STX * STY, 2) k_st3_tma(const __grid_constant_
         st_zdispatch<K>((iz - iz_lo) % K, acc, v, gz, done);
         // the slot just completed began at plane iz - K + 1: output oz
         const int oz = iz - (K - 1) + a.off;
-        if (oz >= oz_lo && y < a.o1) {
+        if (oz >= oz_lo && y < a.o1 && a.pair_store) {
+            // planes, even row length, 8-byte aligned output: the thread's two x neighbours as one 64-bit store per
+            // channel (x0 even, so both are in the row or neither)
+            if (x0 < a.o2) {
+                float2* o = reinterpret_cast<float2*>(a.out + (3 * h) * on + (size_t(oz) * a.o1 + y) * a.o2 + x0);
+                const size_t on2 = on / 2;
+                o[0] = make_float2(done[0], done[1]);
+                o[on2] = make_float2(done[2], done[3]);
+                o[2 * on2] = make_float2(done[4], done[5]);
+            }
+        } else if (oz >= oz_lo && y < a.o1) {
             const size_t row0 = (size_t(oz) * a.o1 + y) * a.o2;
 #pragma unroll
             for (int u = 0; u < 2; ++u) {
@@ -655,6 +676,7 @@ int structure_tensor3_device(const float* vol, unsigned s0, unsigned s1, unsigne
     a.K = int(K); a.off = mode == 0 ? 0 : int(K / 2);
     gaussian1d(K, sigma, a.g);
     a.out = out; a.layout = out_layout;
+    a.pair_store = out_layout == TVGB_LAYOUT_SYM6_PLANES && d[2] % 2 == 0 && reinterpret_cast<uintptr_t>(out) % 8 == 0;
     const unsigned gx = ceil_div(d[2], STX), gy = ceil_div(d[1], STY);
     const bool fixed = K <= unsigned(ST_MAXT);
     const int EX = STX + int(K) - 1, EY = STY + int(K) - 1;
