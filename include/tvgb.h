@@ -256,16 +256,17 @@ int tvgb_tensorvote_sweep(const float* t_in, const float* G, unsigned shape0, un
 
 /* ---- Learned plate / ball vote (no reference counterpart: a learned
  * stand-in for the reference's plate3_numerical_device, tensorvote.h:2457).
- * The network is an MLP 7 -> 64 -> 64 -> 64 -> 6 (GELU; BF16 weights and
- * activations on the tensor cores, FP32 accumulation) from
- * (offset direction o / |o|, plate normal n, flag: 1 plate / 0 ball) to the
+ * The network is an MLP 28 -> 64 -> 64 -> 64 -> 6 (GELU; BF16 weights and
+ * activations on the tensor cores, FP32 accumulation) from the features of
+ * (offset direction d = o / |o|, plate normal n, flag: 1 plate / 0 ball) --
+ * the seven inputs, then d_i d_j and n_i n_j (i <= j) and d_i n_j -- to the
  * vote's angular part (xx, xy, xz, yy, yz, zz) for sigma2 = 0, power 1,
  * o != 0; the Gaussian exp(-|o|^2 / sigma^2) is applied analytically.  Parameters: a
  * float32 vector of tvgb_surrogate_param_count() values, layout
- * W1[64][8] b1[64] W2[64][64] b2[64] W3[64][64] b3[64] W4[8][64] b4[8]
- * (W[out][in]; W1[.][7], W4[6..7][.], b4[6..7] zero).  Arrays are host or
- * device pointers; X and T hold 8 floats per sample (inputs padded with a
- * zero, targets with two). */
+ * W1[64][28] b1[64] W2[64][64] b2[64] W3[64][64] b3[64] W4[8][64] b4[8]
+ * (W[out][in]; W4[6..7][.], b4[6..7] zero).  Arrays are host or device
+ * pointers; X and T hold 8 floats per sample (the seven raw inputs padded
+ * with a zero, targets with two); the features are formed on the device. */
 int tvgb_surrogate_param_count(void);
 
 /* n training samples from the plain orientation integral (64 orientations;
