@@ -451,9 +451,13 @@ struct St3TmaGeom {
     static constexpr int BY = EY + 2;
     static constexpr int SLOT = (BX * BY + 31) / 32 * 32;   // floats per ring slot (128-byte multiples)
     static constexpr uint32_t BOX_BYTES = uint32_t(BX) * BY * 4;
-    // raw ring, products sT[6][EY][EX], y-blurred rows sY[6][8][EX], then the slots' mbarriers
-    static constexpr size_t SMEM =
-        sizeof(float) * (size_t(ST_TMA_SLOTS) * SLOT + 6 * EY * EX + 6 * STY * EX) + 8 * ST_TMA_SLOTS;
+    // channel strides of the products and of the y-blurred rows, padded to EX mod 32 words: a warp's 32
+    // consecutive (channel, column) tasks of the y blur that cross into the next channel then continue on the
+    // next banks instead of meeting their own first lanes (2-way conflicts for 5 of a CTA's 8 warps otherwise)
+    static constexpr int PSP = EY * EX + ((EX - EY * EX) % 32 + 32) % 32;
+    static constexpr int SYP = STY * EX + ((EX - STY * EX) % 32 + 32) % 32;
+    // raw ring, products sT[6][PSP], y-blurred rows sY[6][SYP], then the slots' mbarriers
+    static constexpr size_t SMEM = sizeof(float) * (size_t(ST_TMA_SLOTS) * SLOT + 6 * PSP + 6 * SYP) + 8 * ST_TMA_SLOTS;
 };
 
 static __device__ unsigned g_st3_faults;             // CTAs whose plane wait timed out
@@ -470,8 +474,9 @@ __global__ void __launch_bounds__(STX * STY, 2) k_st3_tma(const __grid_constant_
     extern __shared__ __align__(128) float smem[];
     float* raw = smem;                                   // ST_TMA_SLOTS slots of G::SLOT floats
     float* sT = raw + ST_TMA_SLOTS * G::SLOT;
-    float* sY = sT + 6 * PS;
-    uint64_t* bars = reinterpret_cast<uint64_t*>(sY + 6 * STY * EX);
+    constexpr int PSP = G::PSP, SYP = G::SYP;            // padded channel strides
+    float* sY = sT + 6 * PSP;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(sY + 6 * SYP);
     const int tid = threadIdx.x;
     float gw[K], gz[K];
 #pragma unroll
@@ -543,8 +548,8 @@ __global__ void __launch_bounds__(STX * STY, 2) k_st3_tma(const __grid_constant_
                         const float gx = R1[c + 1] - R1[c - 1];
                         const float gy = R1[c + RX] - R1[c - RX];
                         const float gzv = R2[c] - R0[c];
-                        sT[e] = gx * gx; sT[PS + e] = gx * gy; sT[2 * PS + e] = gx * gzv;
-                        sT[3 * PS + e] = gy * gy; sT[4 * PS + e] = gy * gzv; sT[5 * PS + e] = gzv * gzv;
+                        sT[e] = gx * gx; sT[PSP + e] = gx * gy; sT[2 * PSP + e] = gx * gzv;
+                        sT[3 * PSP + e] = gy * gy; sT[4 * PSP + e] = gy * gzv; sT[5 * PSP + e] = gzv * gzv;
                     }
                 }
             } else {
@@ -561,8 +566,8 @@ __global__ void __launch_bounds__(STX * STY, 2) k_st3_tma(const __grid_constant_
                             gy = grad2(R1[c - RX], R1[c], R1[c + RX], gyp, a.s1);
                             gzv = grad2(R0[c], R1[c], R2[c], iz, a.s0);
                         }
-                        sT[e] = gx * gx; sT[PS + e] = gx * gy; sT[2 * PS + e] = gx * gzv;
-                        sT[3 * PS + e] = gy * gy; sT[4 * PS + e] = gy * gzv; sT[5 * PS + e] = gzv * gzv;
+                        sT[e] = gx * gx; sT[PSP + e] = gx * gy; sT[2 * PSP + e] = gx * gzv;
+                        sT[3 * PSP + e] = gy * gy; sT[4 * PSP + e] = gy * gzv; sT[5 * PSP + e] = gzv * gzv;
                     }
                 }
             }
@@ -572,7 +577,7 @@ __global__ void __launch_bounds__(STX * STY, 2) k_st3_tma(const __grid_constant_
         if (zin) {
             for (int it = tid; it < 6 * EX; it += NT) {
                 const int c = it / EX, rx = it - c * EX;
-                const float* col = sT + c * PS + rx;
+                const float* col = sT + c * PSP + rx;
                 float cv[EY];
 #pragma unroll
                 for (int r = 0; r < EY; ++r) cv[r] = col[r * EX];
@@ -581,7 +586,7 @@ __global__ void __launch_bounds__(STX * STY, 2) k_st3_tma(const __grid_constant_
                     float s = 0.0f;
 #pragma unroll
                     for (int k = 0; k < K; ++k) s = fmaf(gw[k], cv[t + k], s);
-                    sY[(c * STY + t) * EX + rx] = s;
+                    sY[c * SYP + t * EX + rx] = s;
                 }
             }
         }
@@ -590,7 +595,7 @@ __global__ void __launch_bounds__(STX * STY, 2) k_st3_tma(const __grid_constant_
         if (zin) {
 #pragma unroll
             for (int cc = 0; cc < 3; ++cc) {
-                const float2* row = reinterpret_cast<const float2*>(sY + ((3 * h + cc) * STY + ty) * EX + px);
+                const float2* row = reinterpret_cast<const float2*>(sY + (3 * h + cc) * SYP + ty * EX + px);
                 float s0 = 0.0f, s1 = 0.0f;
 #pragma unroll
                 for (int q = 0; q < (K + 1) / 2; ++q) {
