@@ -42,7 +42,7 @@ extern "C" {
 #define TVGB_ERR_ARG 1          /* invalid argument (shape, sigma, window, null pointer) */
 #define TVGB_ERR_CUDA 2         /* CUDA runtime or launch error */
 #define TVGB_ERR_NOMEM 3        /* device allocation failed */
-#define TVGB_ERR_UNSUPPORTED 4  /* valid request this build does not implement */
+#define TVGB_ERR_UNSUPPORTED 4  /* a valid request the library does not implement */
 
 /* layouts / formats */
 #define TVGB_LAYOUT_MAT3 9      /* 9 floats per voxel, AoS */

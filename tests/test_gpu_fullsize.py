@@ -61,7 +61,7 @@ def check_eigenvectors(gvec, rvec, g6, r6, rev, label, c_solver=64.0, min_separa
 
     the first term the two voted tensors' own difference, the second the
     FP32 closed-form solver's rounding.  Where that bound is below 1e-4 rad
-    (well-separated eigenvalues), the benchmark spec's 1e-4 bar applies
+    (well-separated eigenvalues), the 1e-4 parity bar applies
     directly, and at least min_separated of the sample's e2 vectors must be
     in that class so the check is not vacuous.  Against the reference's CPU
     algorithm (parity mode) the two voted tensors differ by ~2e-5 relative
