@@ -688,16 +688,19 @@ __device__ __forceinline__ void vote_row_pk2(const float4* __restrict__ rA, cons
     }
 }
 
-template <bool STICK, bool PLATE, bool BALL>
+template <bool STICK, bool PLATE, bool BALL, bool TBL>
 __global__ void __launch_bounds__(VX * VY, TVGB_FAST_MINB) k_vote3_pk(FastArgs a) {
     constexpr int R = 4;
     constexpr int NQ = BALL ? 4 : 3;         // float4 per paired-table entry
     extern __shared__ __align__(16) float4 smem[];
     const int hw = a.hw;
-    const int nt = 3 * hw * hw + 1;          // radial table entries
     const int ne = 2 * hw * hw + 1;          // paired-table entries (ox^2 + oy^2)
     const int SW = VX + 2 * hw;
     const int SR = VY + a.rows - 1;
+    // TBL: the radial table (2 nt float4) in shared memory.  Without it (the largest windows) each plane's
+    // paired table takes its entries from fast_radial_entry directly (4 ne evaluations per plane and CTA,
+    // under 1% of the plane's work), which leaves room for two CTAs per SM with several voter rows per stage
+    const int nt = TBL ? 3 * hw * hw + 1 : 0;
     float4* tbl = smem;                      // 2 nt
     float4* ptab = tbl + 2 * nt;             // 2 pairs x ne x NQ
     float4* sA = ptab + 2 * ne * NQ;
@@ -748,8 +751,14 @@ __global__ void __launch_bounds__(VX * VY, TVGB_FAST_MINB) k_vote3_pk(FastArgs a
                     const int p = i / ne, e = i - p * ne;
                     const int oa = dzp - 2 * p, ob = oa - 1;
                     float4 ta = make_float4(0, 0, 0, 0), tba = ta, tb = ta, tbb = ta;
-                    if (abs(oa) <= hw) { ta = tbl[2 * (e + oa * oa)]; tba = tbl[2 * (e + oa * oa) + 1]; }
-                    if (abs(ob) <= hw) { tb = tbl[2 * (e + ob * ob)]; tbb = tbl[2 * (e + ob * ob) + 1]; }
+                    if (abs(oa) <= hw) {
+                        if (TBL) { ta = tbl[2 * (e + oa * oa)]; tba = tbl[2 * (e + oa * oa) + 1]; }
+                        else fast_radial_entry(a, e + oa * oa, ta, tba);
+                    }
+                    if (abs(ob) <= hw) {
+                        if (TBL) { tb = tbl[2 * (e + ob * ob)]; tbb = tbl[2 * (e + ob * ob) + 1]; }
+                        else fast_radial_entry(a, e + ob * ob, tb, tbb);
+                    }
                     float4* q = ptab + (size_t(p) * ne + e) * NQ;
                     // radial entry a = (c1, ct g, 2 g, A0), b = (A1, Bp, ball I, ball oo^T)
                     q[0] = make_float4(ta.x, tb.x, ta.y, tb.y);
@@ -1046,22 +1055,27 @@ static size_t fast_smem(int hw, int rows, bool S, bool P, bool B) {
            (B ? size_t(SR) * SW * 4 : 0);
 }
 
-template <bool S, bool P, bool B>
-static int launch_pk_t(const FastArgs& a, size_t smem, cudaStream_t st) {
-    TVGB_CUDA(cudaFuncSetAttribute(k_vote3_pk<S, P, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+template <bool S, bool P, bool B, bool T>
+static int launch_pk_tt(const FastArgs& a, size_t smem, cudaStream_t st) {
+    TVGB_CUDA(cudaFuncSetAttribute(k_vote3_pk<S, P, B, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     dim3 grid(ceil_div(a.s2, VX), ceil_div(a.s1, VY), ceil_div(size_t(a.zr1 - a.zr0), 4));
     {
         KernelTimer kt_("k_vote3_fast", st);
-        k_vote3_pk<S, P, B><<<grid, dim3(VX, VY), smem, st>>>(a);
+        k_vote3_pk<S, P, B, T><<<grid, dim3(VX, VY), smem, st>>>(a);
         kt_.stop();
     }
     TVGB_LAUNCHED();
     return TVGB_OK;
 }
 
-static size_t pk_smem(int hw, int rows, bool S, bool P, bool B) {
-    const size_t ne = size_t(2) * hw * hw + 1;
-    return fast_smem(hw, rows, S, P, B) + 2 * ne * (B ? 4 : 3) * 16;
+template <bool S, bool P, bool B>
+static int launch_pk_t(const FastArgs& a, size_t smem, bool tbl, cudaStream_t st) {
+    return tbl ? launch_pk_tt<S, P, B, true>(a, smem, st) : launch_pk_tt<S, P, B, false>(a, smem, st);
+}
+
+static size_t pk_smem(int hw, int rows, bool S, bool P, bool B, bool tbl) {
+    const size_t ne = size_t(2) * hw * hw + 1, nt = size_t(3) * hw * hw + 1;
+    return fast_smem(hw, rows, S, P, B) - (tbl ? 0 : 2 * nt * 16) + 2 * ne * (B ? 4 : 3) * 16;
 }
 
 static int launch_none(const FastArgs& a, cudaStream_t st) {
@@ -1085,20 +1099,26 @@ static int launch_fast(FastArgs a, bool S, bool P, bool B, cudaStream_t st) {
     const int w = 2 * a.hw + 1;
     const size_t budget = (TVGB_FAST_MINB >= 3 ? 72 : 100) * 1024;
     if (TVGB_PACKED && FAST_R == 4 && (TVGB_PK_BALL || !B)) {
-        int rows = w;
-        while (rows > 1 && pk_smem(a.hw, rows, S, P, B) > budget) rows = (rows + 1) / 2;
-        const size_t smem = pk_smem(a.hw, rows, S, P, B);
+        // two CTAs per SM: 228 KB of shared memory less 1 KB reserved per CTA.  The radial table stays in shared
+        // memory unless leaving it out lets a stage hold more voter rows
+        const size_t pk_budget = (TVGB_FAST_MINB >= 3 ? 72 : 112) * 1024;
+        int rows_t = w, rows_n = w;
+        while (rows_t > 1 && pk_smem(a.hw, rows_t, S, P, B, true) > pk_budget) rows_t = (rows_t + 1) / 2;
+        while (rows_n > 1 && pk_smem(a.hw, rows_n, S, P, B, false) > pk_budget) rows_n = (rows_n + 1) / 2;
+        const bool tbl = rows_t >= rows_n && pk_smem(a.hw, rows_t, S, P, B, true) <= pk_budget;
+        const int rows = tbl ? rows_t : rows_n;
+        const size_t smem = pk_smem(a.hw, rows, S, P, B, tbl);
         if (smem <= 200 * 1024) {
             a.rows = rows;
             const int code = (S ? 4 : 0) | (P ? 2 : 0) | (B ? 1 : 0);
             switch (code) {
-                case 4: return launch_pk_t<true, false, false>(a, smem, st);
-                case 2: return launch_pk_t<false, true, false>(a, smem, st);
-                case 6: return launch_pk_t<true, true, false>(a, smem, st);
-                case 7: return launch_pk_t<true, true, true>(a, smem, st);
-                case 5: return launch_pk_t<true, false, true>(a, smem, st);
-                case 3: return launch_pk_t<false, true, true>(a, smem, st);
-                case 1: return launch_pk_t<false, false, true>(a, smem, st);
+                case 4: return launch_pk_t<true, false, false>(a, smem, tbl, st);
+                case 2: return launch_pk_t<false, true, false>(a, smem, tbl, st);
+                case 6: return launch_pk_t<true, true, false>(a, smem, tbl, st);
+                case 7: return launch_pk_t<true, true, true>(a, smem, tbl, st);
+                case 5: return launch_pk_t<true, false, true>(a, smem, tbl, st);
+                case 3: return launch_pk_t<false, true, true>(a, smem, tbl, st);
+                case 1: return launch_pk_t<false, false, true>(a, smem, tbl, st);
                 default: return TVGB_OK;
             }
         }
