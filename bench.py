@@ -1025,7 +1025,8 @@ def run_c1(args, rank, world, local_rank, emit=True):
     cpu = accuracy = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         from oracle import oracle as O
-        crop = img_np[:192, :192]
+        cs = min(192, size)                                  # crop edge
+        crop = img_np[:cs, :cs]
         t0 = time.perf_counter()
         st_c = O.structure_tensor2(crop, 1.0, 1)
         vo_c = O.tensorvote2(st_c, sigma, 0.0, 1, w, samples=samples)
@@ -1033,19 +1034,20 @@ def run_c1(args, rank, world, local_rank, emit=True):
         th_c = O.evecs2polar(vo_c, e_c)
         tc = time.perf_counter() - t0
         cpu = {"value": crop.size / tc, "unit": "pixels/s", "cores": 1, "kind": "port",
-               "sample": "192x192 crop: the reference's CPU 2D path (tira::cpu::tensorvote's algorithm, single "
+               "sample": f"{cs}x{cs} crop: the reference's CPU 2D path (tira::cpu::tensorvote's algorithm, single "
                          "thread as shipped) incl. structure tensor and eigenpairs"}
         # the crop's interior (its window and blur halo away from the crop's edges) sees the same pixels as
         # the full image: the GPU's end-to-end outputs there against the reference's CPU algorithm
         m = w // 2 + 4
-        g_vo = vo_h[m:192 - m, m:192 - m].reshape(-1, 4).astype(np.float64)
-        r_vo = np.asarray(vo_c)[m:192 - m, m:192 - m].reshape(-1, 4).astype(np.float64)
-        pix = (np.arange(m, 192 - m)[:, None] * size + np.arange(m, 192 - m)[None, :]).ravel()
+    if cpu is not None and cs > 2 * m:
+        g_vo = vo_h[m:cs - m, m:cs - m].reshape(-1, 4).astype(np.float64)
+        r_vo = np.asarray(vo_c)[m:cs - m, m:cs - m].reshape(-1, 4).astype(np.float64)
+        pix = (np.arange(m, cs - m)[:, None] * size + np.arange(m, cs - m)[None, :]).ravel()
         g_ev, r_ev = ev_h[pix].astype(np.float64), np.asarray(e_c).reshape(-1, 2)[
-            (np.arange(m, 192 - m)[:, None] * 192 + np.arange(m, 192 - m)[None, :]).ravel()].astype(np.float64)
+            (np.arange(m, cs - m)[:, None] * cs + np.arange(m, cs - m)[None, :]).ravel()].astype(np.float64)
         g_th = th_h[pix].astype(np.float64)
         r_th = np.asarray(th_c).reshape(-1, 2)[
-            (np.arange(m, 192 - m)[:, None] * 192 + np.arange(m, 192 - m)[None, :]).ravel()].astype(np.float64)
+            (np.arange(m, cs - m)[:, None] * cs + np.arange(m, cs - m)[None, :]).ravel()].astype(np.float64)
         vr = np.linalg.norm(g_vo - r_vo, axis=1) / np.maximum(np.linalg.norm(r_vo, axis=1), 1e-30)
         er = np.abs(g_ev - r_ev).max(axis=1) / np.maximum(np.abs(r_ev).max(axis=1), 1e-30)
         da = np.abs(g_th - r_th) % np.pi                   # eigenvector angles, up to sign
