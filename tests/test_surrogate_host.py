@@ -25,6 +25,38 @@ def test_oracle_gradient_matches_finite_differences():
         assert abs(fd - g[i]) <= 1e-5 * max(abs(fd), 1e-3)
 
 
+def test_oracle_forward_is_the_feature_mlp():
+    """The FP64 oracle's unquantised forward pass is the MLP over the 28
+    features of each sample (x, then d_i d_j and n_i n_j for i <= j, then
+    d_i n_j), restated here in NumPy."""
+    rng = np.random.default_rng(3)
+    P = rng.normal(size=O.mlp_param_count()) * 0.3
+    X = rng.normal(size=(9, 8))
+    X[:, 7] = 0.0
+    _, _, Y = O.mlp_loss_grad(P, X, np.zeros((9, 8)), quant=False)
+    d, n = X[:, :3], X[:, 3:6]
+    iu = [(0, 0), (0, 1), (0, 2), (1, 1), (1, 2), (2, 2)]
+    F = np.concatenate([X[:, :7], np.stack([d[:, i] * d[:, j] for i, j in iu], 1),
+                        np.stack([n[:, i] * n[:, j] for i, j in iu], 1),
+                        np.stack([d[:, i] * n[:, j] for i in range(3) for j in range(3)], 1)], 1)
+    assert F.shape == (9, 28)
+    gelu = lambda z: 0.5 * z * (1.0 + np.tanh(0.7978845608028654 * (z + 0.044715 * z ** 3)))
+    o = 0
+    W1 = P[o:o + 64 * 28].reshape(64, 28); o += 64 * 28
+    b1 = P[o:o + 64]; o += 64
+    W2 = P[o:o + 64 * 64].reshape(64, 64); o += 64 * 64
+    b2 = P[o:o + 64]; o += 64
+    W3 = P[o:o + 64 * 64].reshape(64, 64); o += 64 * 64
+    b3 = P[o:o + 64]; o += 64
+    W4 = P[o:o + 8 * 64].reshape(8, 64); o += 8 * 64
+    b4 = P[o:o + 8]
+    h = gelu(F @ W1.T + b1)
+    h = gelu(h @ W2.T + b2)
+    h = gelu(h @ W3.T + b3)
+    ref = h @ W4.T + b4
+    np.testing.assert_allclose(Y, ref, rtol=1e-12, atol=1e-12)
+
+
 def test_target_is_the_exact_plate_and_ball():
     """64 orientations integrate the degree-4 integrand exactly: the target
     equals the closed forms (sigma2 = 0, Gaussian factored out)."""
